@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Forward + backward throughput of the differentiable rasteriser.
+
+Workload (one step = one forward and one backward over one batch):
+  35,002 V / 70,000 F displaced sphere (mm), 1024^2 texture, textured +
+  SH-shaded, 8 ring views at 1024x1024 (8,388,608 pixels), upstream image
+  gradient N(0,1), no target-image gradient.  Seeded synthetic inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gvr|reference]
+
+One JSON line on rank 0.  `value` is device time with inputs resident in
+HBM (L2 flushed between steps by a 256 MiB memset outside the timed events);
+`e2e` goes through the C ABI with pinned host buffers and the host<->device
+copies inside the timed region.  Under torchrun every rank renders its own
+replica (the path needs no cross-GPU exchange), `value` is the total pixels
+of all ranks / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "gvv-differentiable-cuda-renderer_gb300")
+for _p in (PKG, REPO):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "fwd+bwd Mpix/s (8×1024², 70k faces)"
+UNIT = "Mpix/s"
+WORKLOAD = ("multiview_textured: 35,002 V / 70,000 F displaced sphere (mm), textured 1024^2 + SH shaded, "
+            "8 ring views at 1024x1024, fwd+bwd w.r.t. vertices, texture and SH")
+FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["gvr", "reference"], default="gvr")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bound of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def algorithmic_bytes(P, C, N, F, Ht, Wt, textured, vertex_color):
+    """Bytes one fwd+bwd call must move ('Algorithmic bytes')."""
+    return (P * 64 + C * (12 * N + 12 * F + 24 * F * textured + 12 * N) + 12 * N * vertex_color +
+            24 * Ht * Wt * textured + 24 * N + 216 * C)
+
+
+def kernel_bytes(name, P, C, N, F, Ht, Wt, textured, target):
+    """Algorithmic bytes of one launch of the two pixel kernels."""
+    if name == "k_raster":    # render 12 + face 4 + bary 8 per pixel; vertex normals, faces, uvs, texture read
+        return P * 24 + C * (12 * N + 12 * F + 24 * F * textured) + 12 * Ht * Wt * textured
+    if name == "k_bwd_pixels":  # grad_render 12 + face 4 (+ target and its grad) per pixel; texture grad written
+        return P * (16 + 24 * target) + C * (12 * N + 12 * F + 24 * F * textured) + 24 * Ht * Wt * textured
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        self.t0 = time.time()
+
+    def stop(self):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip().lower() == "active"})
+        load = [s for s in sm if mx and s >= 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_reference(scene, seconds, max_reps=None):
+    """The oracle port (CPU restatement of the reference kernels) on all host
+    cores: full fwd+bwd of the workload, repeated up to `seconds`."""
+    from oracle import oracle
+    from oracle.oracle import OracleScene
+    s = scene
+    o = OracleScene(s["faces"], s["uvs"], s["vertex_pos"][0], s["vertex_color"][0], s["texture"][0],
+                    s["sh_coeff"][0], s["extrinsics"][0], s["intrinsics"][0], s["width"], s["height"],
+                    s["albedo_mode"], s["shading_mode"])
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        out = o.forward()
+        o.backward(out["face"], out["bary"], out["vertex_normal"], s["grad_render"][0], s["target_image"][0],
+                   s["grad_target"][0])
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or (max_reps and reps >= max_reps):
+            break
+    P = s["num_views"] * s["width"] * s["height"]
+    return {"value": P * reps / el / 1e6, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{reps} x the full workload (fwd+bwd, 8 views 1024^2), {el:.1f} s"}
+
+
+def run_reference(args):
+    """The reference has no CPU implementation of this path (its kernels are
+    CUDA only), so this arm times the oracle port of those kernels on every
+    host core.  Each step is a bounded sample of the workload: one of the 8
+    views (cycling) at full resolution, forward + backward."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from gvr import scenes
+    from oracle import oracle
+    from oracle.oracle import OracleScene
+    oracle.build()
+    s = scenes.multiview_textured(seed=0)
+    P1 = s["width"] * s["height"]
+
+    def one_view(c):
+        sl = slice(c, c + 1)
+        o = OracleScene(s["faces"], s["uvs"], s["vertex_pos"][0], s["vertex_color"][0], s["texture"][0],
+                        s["sh_coeff"][0][sl], s["extrinsics"][0][sl], s["intrinsics"][0][sl], s["width"],
+                        s["height"], s["albedo_mode"], s["shading_mode"])
+        out = o.forward()
+        o.backward(out["face"], out["bary"], out["vertex_normal"], s["grad_render"][0][sl], s["target_image"][0][sl],
+                   s["grad_target"][0][sl])
+
+    for k in range(min(args.warmup, 2)):
+        one_view(k % s["num_views"])
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        one_view(k % s["num_views"])
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = P1 / (ms / 1e3) / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch": 1, "views": 8, "resolution": 1024, "faces": 70000,
+                       "vertices": 35002, "texture": 1024, "parallelism": "replicas"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                             "sample": "each step: one of the 8 views (cycling) at 1024^2, fwd+bwd, on the CPU "
+                                       "oracle (the reference has no CPU path; its kernels are CUDA only)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gvr(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from gvr import _lib, native_build, renderer, scenes
+    native_build.build()
+    L = _lib.load()
+
+    s = scenes.multiview_textured(seed=rank)
+    B, C, H, W = 1, s["num_views"], s["height"], s["width"]
+    N, F = s["num_vertices"], s["faces"].shape[0]
+    Ht, Wt = s["texture"].shape[1], s["texture"].shape[2]
+    P = B * C * H * W
+    h = renderer.get_handle(s["faces"], s["uvs"], N, C, W, H, s["albedo_mode"], s["shading_mode"], device=dev)
+    host = {k: torch.from_numpy(np.ascontiguousarray(s[k])).pin_memory()
+            for k in ("vertex_pos", "vertex_color", "texture", "sh_coeff", "extrinsics", "intrinsics", "grad_render")}
+    d = {k: v.to(dev) for k, v in host.items()}
+    out = dict(bary=torch.empty((B, C, H, W, 2), device=dev), face=torch.empty((B, C, H, W), dtype=torch.int32, device=dev),
+               render=torch.empty((B, C, H, W, 3), device=dev), vnorm=torch.empty((B, C, N, 3), device=dev),
+               gpos=torch.empty((B, N, 3), device=dev), gcol=torch.empty((B, N, 3), device=dev),
+               gtex=torch.empty((B, Ht, Wt, 3), device=dev), gsh=torch.empty((B, C, 27), device=dev))
+    fws = torch.empty(h.forward_workspace_size(B), dtype=torch.uint8, device=dev)
+    bws = torch.empty(h.backward_workspace_size(B), dtype=torch.uint8, device=dev)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    fa = _lib.GvrForwardArgs(B, Ht, Wt, p(d["vertex_pos"]), p(d["vertex_color"]), p(d["texture"]), p(d["sh_coeff"]),
+                             None, p(d["extrinsics"]), p(d["intrinsics"]), p(out["bary"]), p(out["face"]),
+                             p(out["render"]), p(out["vnorm"]), None, None, p(fws), fws.numel())
+    ba = _lib.GvrBackwardArgs(B, Ht, Wt, p(d["grad_render"]), p(d["vertex_pos"]), p(d["vertex_color"]), p(d["texture"]),
+                              p(d["sh_coeff"]), None, p(out["vnorm"]), None, p(out["face"]), None, p(d["extrinsics"]),
+                              p(d["intrinsics"]), p(out["gpos"]), p(out["gcol"]), p(out["gtex"]), p(out["gsh"]),
+                              p(bws), bws.numel())
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        _lib.check(L.gvr_forward(h.ptr, ctypes.byref(fa), sp))
+        _lib.check(L.gvr_backward(h.ptr, ctypes.byref(ba), sp))
+
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, device time per step between events
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    n0 = L.gvr_launch_count()
+    t_wall = time.perf_counter()
+    for a, b in evs:
+        flush.zero_()
+        a.record(stream)
+        step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    barrier(world)
+    launches = L.gvr_launch_count() - n0
+    ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    ms = reduce_max(ms, world)
+    value = world * P / (ms / 1e3) / 1e6
+
+    # ---- per-kernel time of the same steps (events around each launch, on the launching stream)
+    L.gvr_profile_enable(1)
+    for _ in range(args.steps):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    prof = _lib.profile_read()
+    L.gvr_profile_enable(0)
+    clk = clocks.stop()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_n, dom_ms) = dom[0], dom[1]
+    dom_avg = dom_ms / max(dom_n, 1)
+    textured = s["albedo_mode"] == "textured"
+    kb = kernel_bytes(dom_name, P, C, N, F, Ht, Wt, textured, 0)
+    peaks = {}
+    pk_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    peak = peaks.get("hbm_gbs") or 6800.0
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    traffic = None
+    tf_path = os.path.join(REPO, "profiles", "dram_traffic.json")
+    if os.path.exists(tf_path):
+        traffic = json.load(open(tf_path)).get(dom_name)
+    achieved = (kb / (dom_avg / 1e3) / 1e9) if kb else None
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "bytes_per_launch": kb, "avg_launch_ms": dom_avg, "peak_source": peak_src}
+    step_bytes = algorithmic_bytes(P, C, N, F, Ht, Wt, int(textured), int(s["albedo_mode"] == "vertexColor"))
+
+    # ---- end to end through the C ABI with host buffers
+    hres = {k: torch.empty(out[k].shape, dtype=out[k].dtype).pin_memory() for k in ("render", "gpos", "gtex", "gsh")}
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    d2h = sum(v.numel() * v.element_size() for v in hres.values())
+
+    def e2e_step():
+        for k, v in host.items():
+            d[k].copy_(v, non_blocking=True)
+        step()
+        for k, v in hres.items():
+            v.copy_(out[k], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world)
+    barrier(world)
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_reference(s, args.cpu_seconds)
+        except Exception as exc:  # the checker is optional for the GPU number
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {exc}"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch": B, "views": C, "resolution": W, "faces": F, "vertices": N,
+                       "texture": Wt, "l2": "flushed between steps (256 MiB memset outside the timed events)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "faces_per_s": world * B * C * F / (ms / 1e3),
+            "step_roofline": {"bytes": step_bytes, "achieved": step_bytes / (ms / 1e3) / 1e9, "peak": peak,
+                              "unit": "GB/s", "frac": step_bytes / (ms / 1e3) / 1e9 / peak},
+            "roofline": roofline,
+            "kernels_ms_per_step": {k: round(v[1] / args.steps, 5) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+            "e2e": {"value": world * P / (e2e_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "timed_wall_s": t_wall,
+            "clocks": clk, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gvr(args)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

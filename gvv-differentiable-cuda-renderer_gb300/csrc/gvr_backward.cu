@@ -1,0 +1,500 @@
+// gvr_backward.cu -- gradients of the render w.r.t. vertex positions,
+// vertex colours, texture and SH coefficients.
+//
+// Reference: renderBuffersGradDevice (cpp/src/Renderer/CUDABasedRasterizationGrad.cu:114-617),
+// one thread per pixel issuing ~210 float atomics per covered pixel.  Here:
+//
+//  k_bwd_pixels  one thread per pixel of a 16x16 tile.  Barycentrics are
+//                recomputed from the face-id buffer with the forward's exact
+//                FP32 ray/triangle arithmetic.  Per pixel the chain rule gives
+//                three 3-vectors weighted by the barycentric of each corner j:
+//                  pos_j = b_j * (m - q)   shading + target-image terms
+//                  gN_j  = b_j * w         d(loss)/d(un-normalised vertex normal)
+//                  col_j = b_j * c         vertex colour
+//                The warp pre-reduces them per face id (__match_any_sync +
+//                a shuffle tree) and one lane per face adds them to a per-face
+//                accumulator with 16-byte vector atomics.  SH gradients are
+//                block-reduced into per-tile partials; texels get atomics.
+//  k_gather_a    per vertex, over its CSR faces: colour grad, position grad
+//                (direct terms) and the vertex-normal gradient gN[v].
+//  k_gather_b    per vertex: the normal-adjacency term of :559-615.  The
+//                reference applies, for every pixel, each corner's weight to
+//                every face around that corner (~162 atomics); that sum is
+//                linear in gN, so per face f=(a0,a1,a2) with
+//                s_f = sum of gN over f's distinct vertices, corner r gets
+//                (v[a(r+1)] - v[a(r+2)]) x s_f (= s_f . d cross(v1-v0, v2-v0)/d v_r).
+//  k_sh_finalize sums the per-tile SH partials in FP64 in a fixed order.
+//
+// The shading-term Jacobian dJBCDVerpos (cpp/src/Utils/RendererUtil.h:670-861)
+// is d(barycentrics)/d(vertices) for a fixed ray.  With e1 = v1-v0,
+// e2 = v2-v0, N = e1 x e2 and the hit point o + t d, implicit
+// differentiation of  b1 e1 + b2 e2 - t d = o - v0  gives
+//   d b1 / d v_j = -b_j (e2 x d)/(N.d),  d b2 / d v_j = -b_j (d x e1)/(N.d),
+//   d b0 / d v_j = -(d b1 + d b2)/d v_j,
+// the same matrix in closed form; the reference's early-out
+// (|cos(d, N)| < 0.001 or |N.N|^2 < 0.001) is kept.
+#include "gvr_internal.cuh"
+#include "gvr_kernels.h"
+#include "gvr_profile.h"
+
+namespace gvr {
+
+// Sum of `val` over the lanes that share `peers` (a __match_any_sync mask):
+// a pointer-jumping tree over the members, log2(largest group) steps.
+// The result is valid in the group's lowest lane.
+template <int NV>
+__device__ __forceinline__ void group_reduce(float (&val)[NV], unsigned peers, int lane) {
+    const unsigned full = 0xffffffffu;
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    const int maxSize = __reduce_max_sync(full, (unsigned)__popc(peers));
+    const unsigned above = peers & ~((2u << lane) - 1u);
+    int ptr = above ? __ffs(above) - 1 : -1;  // lane of the member with rank + d
+    for (int d = 1; d < maxSize; d <<= 1) {
+        const int src = ptr >= 0 ? ptr : lane;
+        const bool take = ptr >= 0 && (rank & (2 * d - 1)) == 0;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            float o = __shfl_sync(full, val[k], src);
+            if (take) val[k] += o;
+        }
+        int nxt = __shfl_sync(full, ptr, src);
+        ptr = ptr >= 0 ? nxt : -1;
+    }
+}
+
+struct BwdIO {
+    const float *grad_render;  // [B,C,H,W,3]
+    const float *verts;        // [B,N,3]
+    const float *colors;       // [B,N,3]
+    const float *texture;      // [B,Ht,Wt,3]
+    const float *sh;           // [B,C,27]
+    const float *target;       // [B,C,H,W,3]
+    const float *vnormal;      // [B,C,N,3]
+    const float *bary_in;      // [B,C,H,W,2] or null
+    const int32_t *face;       // [B,C,H,W]
+    const float *grad_target;  // [B,C,H,W,3] or null
+    float *tex_grad;           // [B,Ht,Wt,3]
+    int imageFilter;
+};
+
+template <int MODE, bool SHADED, bool TARGET>
+__global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
+                                                         const BwdIO io) {
+    constexpr bool COL = MODE == GVR_ALBEDO_VERTEX_COLOR;
+    constexpr bool POS = SHADED || TARGET;
+    constexpr int NPOS = POS ? 9 : 0, NGN = SHADED ? 9 : 0, NCOL = COL ? 9 : 0;
+    constexpr int NV = NPOS + NGN + NCOL > 0 ? NPOS + NGN + NCOL : 1;
+
+    const int T = dims.tilesX * dims.tilesY;
+    const int tile = blockIdx.x % T, bc = blockIdx.x / T, b = bc / dims.C;
+    const int tileX0 = (tile % dims.tilesX) * kTile, tileY0 = (tile / dims.tilesX) * kTile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int u = tileX0 + (tid & (kTile - 1)), v = tileY0 + tid / kTile;
+    const bool inImage = u < dims.W && v < dims.H;
+    const size_t p = ((size_t)bc * dims.H + v) * dims.W + u;
+    const int F = topo.F, N = topo.N;
+
+    int f = inImage ? io.face[p] : -1;
+    if (f >= F) f = -1;  // ids outside [0, F) carry no face
+    float val[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) val[k] = 0.0f;
+    float shv[SHADED ? 27 : 1];
+#pragma unroll
+    for (int k = 0; k < (SHADED ? 27 : 1); ++k) shv[k] = 0.0f;
+
+    if (f >= 0) {
+        const Camera &cam = ws.cams[bc];
+        const V3 origS = v3(cam.origS[0], cam.origS[1], cam.origS[2]);
+        const V3 d = pixel_ray(cam, u, v);
+        const FaceSetup fs = load_face(&ws.geo[(size_t)b * F + f]);
+        V3 abc = barycentric(fs, origS, xdot(origS, fs.n), d);
+        if (abc.x == -1.0f && abc.y == -1.0f && abc.z == -1.0f) {
+            // face buffer inconsistent with the geometry: fall back to the stored barycentrics
+            if (io.bary_in) {
+                float2 bb = reinterpret_cast<const float2 *>(io.bary_in)[p];
+                abc = v3(bb.x, bb.y, xs(xs(1.0f, bb.x), bb.y));
+            } else {
+                f = -1;
+            }
+        }
+        if (f >= 0) {
+            const int i0 = topo.faces[3 * f], i1 = topo.faces[3 * f + 1], i2 = topo.faces[3 * f + 2];
+            const float *VN = io.vnormal + (size_t)bc * N * 3;
+            const V3 N0 = ld3(VN + 3 * i0), N1 = ld3(VN + 3 * i1), N2 = ld3(VN + 3 * i2);
+            const V3 un = pixel_normal_un(N0, N1, N2, abc);
+            const float len = __fsqrt_rn(xdot(un, un));
+            V3 n = v3(xd(un.x, len), xd(un.y, len), xd(un.z, len));
+            const bool flipped = xdot(n, d) > 0.0f;
+            if (flipped) n = v3(-n.x, -n.y, -n.z);
+            const float *gr = io.grad_render + 3 * p;
+            const float G[3] = {gr[0], gr[1], gr[2]};
+            const float *sh = io.sh + (size_t)bc * 27;
+            float basis[9];
+            sh_basis(n, basis);
+            float JCoAl[3] = {1.0f, 1.0f, 1.0f};
+            if (SHADED) {
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                    float l = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) l += sh[9 * ch + k] * basis[k];
+                    JCoAl[ch] = l;
+                }
+            }
+            // albedo as the gradient sees it (CUDABasedRasterizationGrad.cu:274-319)
+            float alb[3] = {0.0f, 0.0f, 0.0f};
+            if (MODE == GVR_ALBEDO_VERTEX_COLOR) {
+                const float *Cb = io.colors + (size_t)b * N * 3;
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch)
+                    alb[ch] = abc.x * Cb[3 * i0 + ch] + abc.y * Cb[3 * i1 + ch] + abc.z * Cb[3 * i2 + ch];
+            }
+            if (MODE == GVR_ALBEDO_TEXTURED) {
+                const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+                const int iu = __float2int_rz(xs(tc.x, 0.5f)), iv = __float2int_rz(xs(tc.y, 0.5f));
+                const int hu = min(iu + 1, dims.Wt - 1), hv = min(iv + 1, dims.Ht - 1);
+                const float LU = iu + 0.5f, HU = iu + 1.5f, LV = iv + 0.5f, HV = iv + 1.5f;
+                const float *tex = io.texture + (size_t)b * dims.Ht * dims.Wt * 3;
+                const float *cLL = tex + ((size_t)iv * dims.Wt + iu) * 3, *cHL = tex + ((size_t)iv * dims.Wt + hu) * 3;
+                const float *cLH = tex + ((size_t)hv * dims.Wt + iu) * 3, *cHH = tex + ((size_t)hv * dims.Wt + hu) * 3;
+                // corner weights exactly as written at CUDABasedRasterizationGrad.cu:311-312
+                const float wv0 = tc.y - LV, wv1 = HV - tc.y, wu0 = tc.x - LU, wu1 = HU - tc.x;
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch)
+                    alb[ch] = wv0 * (wu0 * cLL[ch] + wu1 * cHL[ch]) + wv1 * (wu0 * cLH[ch] + wu1 * cHH[ch]);
+                if (!flipped) {
+                    float *tg = io.tex_grad + (((size_t)b * dims.Ht + iv) * dims.Wt + iu) * 3;
+                    atomicAdd(tg + 0, G[0] * JCoAl[0]);
+                    atomicAdd(tg + 1, G[1] * JCoAl[1]);
+                    atomicAdd(tg + 2, G[2] * JCoAl[2]);
+                }
+            }
+            // Pv: per-pixel vector applied with the stored barycentrics (target term);
+            // Qv[j]: shading term already weighted for corner j
+            float Pv[3] = {0.0f, 0.0f, 0.0f}, wv[3] = {0.0f, 0.0f, 0.0f};
+            float Qv[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+            if (SHADED) {
+                const float ga[3] = {G[0] * alb[0], G[1] * alb[1], G[2] * alb[2]};
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) shv[9 * ch + k] = ga[ch] * basis[k];
+                // ga . d(light)/d(n)  (getJLiNo, RendererUtil.h:371-391)
+                float wt[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                    const float *c9 = sh + 9 * ch;
+                    wt[0] += ga[ch] * (c9[3] + c9[4] * n.y + c9[7] * n.z + 2.0f * c9[8] * n.x);
+                    wt[1] += ga[ch] * (c9[1] + c9[4] * n.x + c9[5] * n.z - 2.0f * c9[8] * n.y);
+                    wt[2] += ga[ch] * (c9[2] + c9[5] * n.y + 6.0f * c9[6] * n.z + c9[7] * n.x);
+                }
+                // . d(n)/d(un) = (|un|^2 I - un un^T) / |un|^3  (getJNoNu, :398-415)
+                const float len2 = len * len, inv3 = 1.0f / (len2 * len);
+                const float wdot = wt[0] * un.x + wt[1] * un.y + wt[2] * un.z;
+                wv[0] = (wt[0] * len2 - un.x * wdot) * inv3;
+                wv[1] = (wt[1] * len2 - un.y * wdot) * inv3;
+                wv[2] = (wt[2] * len2 - un.z * wdot) * inv3;
+                // shading term through the barycentrics (:478-522)
+                const float r0 = wv[0] * N0.x + wv[1] * N0.y + wv[2] * N0.z;
+                const float r1 = wv[0] * N1.x + wv[1] * N1.y + wv[2] * N1.z;
+                const float r2 = wv[0] * N2.x + wv[1] * N2.y + wv[2] * N2.z;
+                const float *Vb = io.verts + (size_t)b * N * 3;
+                const float3 V0 = make_float3(Vb[3 * i0], Vb[3 * i0 + 1], Vb[3 * i0 + 2]);
+                const float3 e1 = make_float3(Vb[3 * i1] - V0.x, Vb[3 * i1 + 1] - V0.y, Vb[3 * i1 + 2] - V0.z);
+                const float3 e2 = make_float3(Vb[3 * i2] - V0.x, Vb[3 * i2 + 1] - V0.y, Vb[3 * i2 + 2] - V0.z);
+                const float Nf[3] = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+                // N.d and the hit point in compensated arithmetic: near grazing
+                // incidence both cancel badly in plain FP32 (error ~ eps/cos) and
+                // the Jacobian scales with 1/cos.
+                const float dv[3] = {d.x, d.y, d.z};
+                const float nd = dot2<3>(Nf, dv);
+                const float nn = Nf[0] * Nf[0] + Nf[1] * Nf[1] + Nf[2] * Nf[2];
+                const float dd = d.x * d.x + d.y * d.y + d.z * d.z;
+                if (nd * nd >= 1.0e-6f * nn * dd && nn * nn >= 0.001f) {
+                    // P - V0 = t d - (V0 - o),  t = N.(V0 - o) / N.d, with V0 - o split exactly
+                    float Dh[3], Dl[3];
+                    two_sum(V0.x, -cam.orig[0], Dh[0], Dl[0]);
+                    two_sum(V0.y, -cam.orig[1], Dh[1], Dl[1]);
+                    two_sum(V0.z, -cam.orig[2], Dh[2], Dl[2]);
+                    const float N6[6] = {Nf[0], Nf[1], Nf[2], Nf[0], Nf[1], Nf[2]};
+                    const float D6[6] = {Dh[0], Dh[1], Dh[2], Dl[0], Dl[1], Dl[2]};
+                    const float t = dot2<6>(N6, D6) / nd;
+                    const float wx = __fmaf_rn(t, d.x, -Dh[0]) - Dl[0];
+                    const float wy = __fmaf_rn(t, d.y, -Dh[1]) - Dl[1];
+                    const float wz = __fmaf_rn(t, d.z, -Dh[2]) - Dl[2];
+                    // barycentrics of the hit point: b1 = (w x e2).N / N.N, b2 = (e1 x w).N / N.N
+                    const float inn = 1.0f / nn;
+                    const float hb1 = ((wy * e2.z - wz * e2.y) * Nf[0] + (wz * e2.x - wx * e2.z) * Nf[1] +
+                                       (wx * e2.y - wy * e2.x) * Nf[2]) * inn;
+                    const float hb2 = ((e1.y * wz - e1.z * wy) * Nf[0] + (e1.z * wx - e1.x * wz) * Nf[1] +
+                                       (e1.x * wy - e1.y * wx) * Nf[2]) * inn;
+                    const float hb[3] = {1.0f - hb1 - hb2, hb1, hb2};
+                    const float inv = 1.0f / nd;
+                    const float3 g1 = make_float3((e2.y * d.z - e2.z * d.y) * inv, (e2.z * d.x - e2.x * d.z) * inv,
+                                                  (e2.x * d.y - e2.y * d.x) * inv);
+                    const float3 g2 = make_float3((d.y * e1.z - d.z * e1.y) * inv, (d.z * e1.x - d.x * e1.z) * inv,
+                                                  (d.x * e1.y - d.y * e1.x) * inv);
+                    const float k1 = r1 - r0, k2 = r2 - r0;
+                    const float q[3] = {k1 * g1.x + k2 * g2.x, k1 * g1.y + k2 * g2.y, k1 * g1.z + k2 * g2.z};
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) Qv[j][a] = -hb[j] * q[a];
+                }
+            }
+            if (TARGET) {
+                // model-to-data term (:531-555): g_target . dT/d(u,v) . d(u,v)/dX . dX/dv_j
+                const float *gt = io.grad_target + 3 * p;
+                const float GT[3] = {gt[0], gt[1], gt[2]};
+                const int k = io.imageFilter;
+                if ((GT[0] != 0.0f || GT[1] != 0.0f || GT[2] != 0.0f) && u >= k + 1 && v >= k + 1 &&
+                    u < dims.W - (k + 1) && v < dims.H - (k + 1)) {
+                    const float *img = io.target + (size_t)bc * dims.H * dims.W * 3;
+                    float gu = 0.0f, gv = 0.0f, norm = 0.0f;
+                    for (int y = -k; y <= k; ++y)
+                        for (int x = -k; x <= k; ++x) {
+                            const int den = x * x + y * y;
+                            if (den == 0) continue;
+                            const float Gu = (float)x / (float)den, Gv = (float)y / (float)den;
+                            const float *I = img + ((size_t)(v + y) * dims.W + (u + x)) * 3;
+                            const float gi = GT[0] * I[0] + GT[1] * I[1] + GT[2] * I[2];
+                            gu += gi * Gu;
+                            gv += gi * Gv;
+                            norm += fabsf(Gu);
+                        }
+                    gu /= norm;
+                    gv /= norm;
+                    const float *Vb = io.verts + (size_t)b * N * 3;
+                    float X[3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) X[a] = abc.x * Vb[3 * i0 + a] + abc.y * Vb[3 * i1 + a] + abc.z * Vb[3 * i2 + a];
+                    const float *KE = cam.KE;
+                    const float Px = KE[0] * X[0] + KE[1] * X[1] + KE[2] * X[2] + KE[3];
+                    const float Py = KE[4] * X[0] + KE[5] * X[1] + KE[6] * X[2] + KE[7];
+                    const float Pz = KE[8] * X[0] + KE[9] * X[1] + KE[10] * X[2] + KE[11];
+                    if (fabsf(Pz) > 0.0001f) {
+                        const float iz = 1.0f / Pz, ax = Px * iz, ay = Py * iz;
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            Pv[a] += (gu * (KE[a] - ax * KE[8 + a]) + gv * (KE[4 + a] - ay * KE[8 + a])) * iz;
+                    }
+                }
+            }
+            const float bw[3] = {abc.x, abc.y, abc.z};
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    if (POS) val[3 * j + a] = bw[j] * Pv[a] + Qv[j][a];
+                    if (SHADED) val[NPOS + 3 * j + a] = bw[j] * wv[a];
+                    if (COL) val[NPOS + NGN + 3 * j + a] = bw[j] * (G[a] * JCoAl[a]);
+                }
+        }
+    }
+
+    // ---- per-face pre-reduction and accumulation
+    if (NPOS + NGN + NCOL > 0) {
+        const unsigned peers = __match_any_sync(0xffffffffu, f);
+        group_reduce<NV>(val, peers, lane);
+        const bool leader = (peers & ((1u << lane) - 1u)) == 0;
+        if (leader && f >= 0) {
+            float4 *acc = ws.faceAcc + ((size_t)b * F + f) * (kFaceAccFloats / 4);
+            if (POS || SHADED) {
+                float a[20];
+#pragma unroll
+                for (int k = 0; k < 20; ++k) a[k] = 0.0f;
+#pragma unroll
+                for (int k = 0; k < NPOS; ++k) a[k] = val[k];
+#pragma unroll
+                for (int k = 0; k < NGN; ++k) a[9 + k] = val[NPOS + k];
+                constexpr int nA = SHADED ? 5 : 3;
+#pragma unroll
+                for (int q = 0; q < nA; ++q) atomicAdd(acc + q, make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]));
+            }
+            if (COL) {
+                float a[12];
+#pragma unroll
+                for (int k = 0; k < 12; ++k) a[k] = 0.0f;
+#pragma unroll
+                for (int k = 0; k < NCOL; ++k) a[k] = val[NPOS + NGN + k];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) atomicAdd(acc + 5 + q, make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]));
+            }
+        }
+    }
+
+    // ---- SH partial sums of this tile
+    if (SHADED) {
+        __shared__ float red[kTilePix / 32][27];
+#pragma unroll
+        for (int k = 0; k < 27; ++k) {
+            float x = shv[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) red[warp][k] = x;
+        }
+        __syncthreads();
+        if (tid < 27) {
+            float s = 0.0f;
+#pragma unroll
+            for (int w = 0; w < kTilePix / 32; ++w) s += red[w][tid];
+            ws.shPartial[((size_t)bc * T + tile) * 27 + tid] = s;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------- vertex gathers
+
+// Face-accumulator layout (floats): [0..8] position grad of corners 0..2,
+// [9..17] vertex-normal grad of corners 0..2, [20..28] colour grad of corners 0..2.
+__global__ void k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc, float *__restrict__ vpos_grad,
+                           float *__restrict__ vcol_grad, float4 *__restrict__ gN, int useCol, int useGN) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = topo.N, F = topo.F;
+    if (i >= B * N) return;
+    int b = i / N, v = i - b * N;
+    float pos[3] = {0, 0, 0}, gn[3] = {0, 0, 0}, col[3] = {0, 0, 0};
+    for (int k = topo.vstart[v]; k < topo.vstart[v + 1]; ++k) {
+        int f = topo.vfaces[k];
+        const float *A = faceAcc + ((size_t)b * F + f) * kFaceAccFloats;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            if (topo.faces[3 * f + r] != v) continue;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                pos[a] += A[3 * r + a];
+                gn[a] += A[9 + 3 * r + a];
+                col[a] += A[20 + 3 * r + a];
+            }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        vpos_grad[3 * (size_t)i + a] = pos[a];
+        vcol_grad[3 * (size_t)i + a] = useCol ? col[a] : 0.0f;
+    }
+    if (useGN) gN[i] = make_float4(gn[0], gn[1], gn[2], 0.0f);
+}
+
+__global__ void k_gather_b(const Topology topo, int B, const float *__restrict__ verts, const float4 *__restrict__ gN,
+                           float *__restrict__ vpos_grad) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = topo.N;
+    if (i >= B * N) return;
+    int b = i / N, v = i - b * N;
+    const float *V = verts + (size_t)b * N * 3;
+    const float4 *g = gN + (size_t)b * N;
+    float acc[3] = {0, 0, 0};
+    for (int k = topo.vstart[v]; k < topo.vstart[v + 1]; ++k) {
+        int f = topo.vfaces[k];
+        int a[3] = {topo.faces[3 * f], topo.faces[3 * f + 1], topo.faces[3 * f + 2]};
+        float4 s = g[a[0]];
+        if (a[1] != a[0]) { float4 t = g[a[1]]; s.x += t.x; s.y += t.y; s.z += t.z; }
+        if (a[2] != a[0] && a[2] != a[1]) { float4 t = g[a[2]]; s.x += t.x; s.y += t.y; s.z += t.z; }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            if (a[r] != v) continue;
+            const float *p1 = V + 3 * a[(r + 1) % 3], *p2 = V + 3 * a[(r + 2) % 3];
+            float e[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
+            acc[0] += e[1] * s.z - e[2] * s.y;
+            acc[1] += e[2] * s.x - e[0] * s.z;
+            acc[2] += e[0] * s.y - e[1] * s.x;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) vpos_grad[3 * (size_t)i + a] += acc[a];
+}
+
+// One block per (batch, view): thread i sums tiles i, i+256, ... for all 27
+// coefficients in FP64, then a fixed-order tree finishes (deterministic).
+__global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
+                                                     int tilesPerView, int shaded) {
+    __shared__ double red[8][27];
+    const int bc = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double s[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) s[k] = 0.0;
+    if (shaded)
+        for (int t = threadIdx.x; t < tilesPerView; t += 256) {
+            const float *p = partial + ((size_t)bc * tilesPerView + t) * 27;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) s[k] += (double)p[k];
+        }
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        double x = s[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        double tot = 0.0;
+        for (int w = 0; w < 8; ++w) tot += red[w][threadIdx.x];
+        sh_grad[(size_t)bc * 27 + threadIdx.x] = (float)tot;
+    }
+}
+
+// ---------------------------------------------------------------------------- host launch
+
+static inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
+
+template <int MODE, bool SHADED, bool TARGET>
+static cudaError_t launch_pixels_t(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const BwdIO &io,
+                                   cudaStream_t st) {
+    const int grid = dims.B * dims.C * dims.tilesX * dims.tilesY;
+    GVR_LAUNCH(st, "k_bwd_pixels", (k_bwd_pixels<MODE, SHADED, TARGET><<<grid, kTilePix, 0, st>>>(topo, dims, ws, io)));
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_pixels_m(bool shaded, bool target, const Topology &topo, const FrameDims &dims,
+                                   const BwdScratch &ws, const BwdIO &io, cudaStream_t st) {
+    if (shaded) return target ? launch_pixels_t<MODE, true, true>(topo, dims, ws, io, st)
+                              : launch_pixels_t<MODE, true, false>(topo, dims, ws, io, st);
+    return target ? launch_pixels_t<MODE, false, true>(topo, dims, ws, io, st)
+                  : launch_pixels_t<MODE, false, false>(topo, dims, ws, io, st);
+}
+
+cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const GvrBackwardArgs &a,
+                            int imageFilter, cudaStream_t st) {
+    const int B = dims.B, C = dims.C, N = topo.N, F = topo.F, T = dims.tilesX * dims.tilesY;
+    const size_t texBytes = (size_t)B * dims.Ht * dims.Wt * 3 * sizeof(float);
+    cudaError_t err;
+    if (dims.albedo == GVR_ALBEDO_NORMAL || dims.albedo == GVR_ALBEDO_LIGHTING) {
+        // python/CudaRenderer.py:207-213: zero gradients for these modes
+        if ((err = cudaMemsetAsync(a.vertex_pos_grad, 0, (size_t)B * N * 3 * sizeof(float), st))) return err;
+        if ((err = cudaMemsetAsync(a.vertex_color_grad, 0, (size_t)B * N * 3 * sizeof(float), st))) return err;
+        if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
+        return cudaMemsetAsync(a.sh_coeff_grad, 0, (size_t)B * C * 27 * sizeof(float), st);
+    }
+    const bool shaded = dims.shading == GVR_SHADING_SHADED && dims.albedo != GVR_ALBEDO_FOREGROUND_MASK;
+    const bool target = a.target_grad != nullptr;
+    if ((err = cudaMemsetAsync(ws.faceAcc, 0, (size_t)B * F * kFaceAccFloats * sizeof(float), st))) return err;
+    if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
+    if ((err = launch_cameras(a.extrinsics, a.intrinsics, ws.cams, B * C, st))) return err;
+    if ((err = launch_face_geo(a.vertex_pos, topo, ws.geo, nullptr, B, st))) return err;
+    BwdIO io{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image, a.vertex_normal,
+             a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter};
+    switch (dims.albedo) {
+        case GVR_ALBEDO_VERTEX_COLOR: err = launch_pixels_m<GVR_ALBEDO_VERTEX_COLOR>(shaded, target, topo, dims, ws, io, st); break;
+        case GVR_ALBEDO_TEXTURED: err = launch_pixels_m<GVR_ALBEDO_TEXTURED>(shaded, target, topo, dims, ws, io, st); break;
+        default: err = launch_pixels_m<GVR_ALBEDO_FOREGROUND_MASK>(false, target, topo, dims, ws, io, st); break;
+    }
+    if (err) return err;
+    GVR_LAUNCH(st, "k_gather_a",
+               k_gather_a<<<blocks((size_t)B * N, 256), 256, 0, st>>>(
+                   topo, B, reinterpret_cast<const float *>(ws.faceAcc), a.vertex_pos_grad, a.vertex_color_grad, ws.gN,
+                   dims.albedo == GVR_ALBEDO_VERTEX_COLOR, shaded));
+    if ((err = cudaGetLastError())) return err;
+    if (shaded) {
+        GVR_LAUNCH(st, "k_gather_b",
+                   k_gather_b<<<blocks((size_t)B * N, 256), 256, 0, st>>>(topo, B, a.vertex_pos, ws.gN, a.vertex_pos_grad));
+        if ((err = cudaGetLastError())) return err;
+    }
+    GVR_LAUNCH(st, "k_sh_finalize", k_sh_finalize<<<B * C, 256, 0, st>>>(ws.shPartial, a.sh_coeff_grad, T, shaded));
+    return cudaGetLastError();
+}
+
+}  // namespace gvr

@@ -1,0 +1,386 @@
+// gvr_forward.cu -- forward render: cameras, face setup, vertex stage and
+// tile binning; the raster + resolve + shade kernel is in gvr_raster.cu.
+//
+// Pipeline for all B x C views of one call (reference: the 7-kernel chain
+// of cpp/src/Renderer/CUDABasedRasterization.cu:449-473, launched once per
+// batch element there):
+//   k_cameras     camera inverses (:23-67)                       B*C threads
+//   k_face_geo    scaled face geometry + face normals (:122-141)  B*F threads
+//   k_vertices    vertex normals (:148-174) + projection (:98-115) B*N threads
+//   k_bin_count   face boxes (:184-208), screen-space skip-test
+//                 constants, per-tile counts                     B*C*F threads
+//   k_scan_tiles  exclusive scan of the tile counts              1 block
+//   k_bin_fill    per-tile face lists                            B*C*F threads
+//   k_raster      one 16x16 tile per block (replaces :215-408)
+#include "gvr_internal.cuh"
+#include "gvr_kernels.h"
+#include "gvr_profile.h"
+
+namespace gvr {
+
+// ---------------------------------------------------------------------------- cameras
+
+__device__ static void mat4_mul_x(const float *a, const float *b, float *r) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            r[4 * i + j] = xa(xa(xa(xm(a[4 * i + 0], b[j]), xm(a[4 * i + 1], b[4 + j])), xm(a[4 * i + 2], b[8 + j])),
+                              xm(a[4 * i + 3], b[12 + j]));
+}
+
+// T3(a,b,c) = (a*b)*c, evaluated left to right as the reference's products.
+__device__ __forceinline__ float T3(float a, float b, float c) { return xm(xm(a, b), c); }
+
+// Cofactor inverse of a row-major 4x4 (float4x4::getInverse,
+// cpp/src/Utils/float4x4.h:160-282): the same cofactor expressions summed
+// left to right, then multiplied by 1/det.
+__device__ static void mat4_inverse_x(const float *e, float *out) {
+    float inv[16];
+    inv[0] = xs(xa(xa(xs(xs(T3(e[5], e[10], e[15]), T3(e[5], e[11], e[14])), T3(e[9], e[6], e[15])), T3(e[9], e[7], e[14])),
+                   T3(e[13], e[6], e[11])), T3(e[13], e[7], e[10]));
+    inv[4] = xa(xs(xs(xa(xa(-T3(e[4], e[10], e[15]), T3(e[4], e[11], e[14])), T3(e[8], e[6], e[15])), T3(e[8], e[7], e[14])),
+                   T3(e[12], e[6], e[11])), T3(e[12], e[7], e[10]));
+    inv[8] = xs(xa(xa(xs(xs(T3(e[4], e[9], e[15]), T3(e[4], e[11], e[13])), T3(e[8], e[5], e[15])), T3(e[8], e[7], e[13])),
+                   T3(e[12], e[5], e[11])), T3(e[12], e[7], e[9]));
+    inv[12] = xa(xs(xs(xa(xa(-T3(e[4], e[9], e[14]), T3(e[4], e[10], e[13])), T3(e[8], e[5], e[14])), T3(e[8], e[6], e[13])),
+                    T3(e[12], e[5], e[10])), T3(e[12], e[6], e[9]));
+    inv[1] = xa(xs(xs(xa(xa(-T3(e[1], e[10], e[15]), T3(e[1], e[11], e[14])), T3(e[9], e[2], e[15])), T3(e[9], e[3], e[14])),
+                   T3(e[13], e[2], e[11])), T3(e[13], e[3], e[10]));
+    inv[5] = xs(xa(xa(xs(xs(T3(e[0], e[10], e[15]), T3(e[0], e[11], e[14])), T3(e[8], e[2], e[15])), T3(e[8], e[3], e[14])),
+                   T3(e[12], e[2], e[11])), T3(e[12], e[3], e[10]));
+    inv[9] = xa(xs(xs(xa(xa(-T3(e[0], e[9], e[15]), T3(e[0], e[11], e[13])), T3(e[8], e[1], e[15])), T3(e[8], e[3], e[13])),
+                   T3(e[12], e[1], e[11])), T3(e[12], e[3], e[9]));
+    inv[13] = xs(xa(xa(xs(xs(T3(e[0], e[9], e[14]), T3(e[0], e[10], e[13])), T3(e[8], e[1], e[14])), T3(e[8], e[2], e[13])),
+                    T3(e[12], e[1], e[10])), T3(e[12], e[2], e[9]));
+    inv[2] = xs(xa(xa(xs(xs(T3(e[1], e[6], e[15]), T3(e[1], e[7], e[14])), T3(e[5], e[2], e[15])), T3(e[5], e[3], e[14])),
+                   T3(e[13], e[2], e[7])), T3(e[13], e[3], e[6]));
+    inv[6] = xa(xs(xs(xa(xa(-T3(e[0], e[6], e[15]), T3(e[0], e[7], e[14])), T3(e[4], e[2], e[15])), T3(e[4], e[3], e[14])),
+                   T3(e[12], e[2], e[7])), T3(e[12], e[3], e[6]));
+    inv[10] = xs(xa(xa(xs(xs(T3(e[0], e[5], e[15]), T3(e[0], e[7], e[13])), T3(e[4], e[1], e[15])), T3(e[4], e[3], e[13])),
+                    T3(e[12], e[1], e[7])), T3(e[12], e[3], e[5]));
+    inv[14] = xa(xs(xs(xa(xa(-T3(e[0], e[5], e[14]), T3(e[0], e[6], e[13])), T3(e[4], e[1], e[14])), T3(e[4], e[2], e[13])),
+                    T3(e[12], e[1], e[6])), T3(e[12], e[2], e[5]));
+    inv[3] = xa(xs(xs(xa(xa(-T3(e[1], e[6], e[11]), T3(e[1], e[7], e[10])), T3(e[5], e[2], e[11])), T3(e[5], e[3], e[10])),
+                   T3(e[9], e[2], e[7])), T3(e[9], e[3], e[6]));
+    inv[7] = xs(xa(xa(xs(xs(T3(e[0], e[6], e[11]), T3(e[0], e[7], e[10])), T3(e[4], e[2], e[11])), T3(e[4], e[3], e[10])),
+                   T3(e[8], e[2], e[7])), T3(e[8], e[3], e[6]));
+    inv[11] = xa(xs(xs(xa(xa(-T3(e[0], e[5], e[11]), T3(e[0], e[7], e[9])), T3(e[4], e[1], e[11])), T3(e[4], e[3], e[9])),
+                    T3(e[8], e[1], e[7])), T3(e[8], e[3], e[5]));
+    inv[15] = xs(xa(xa(xs(xs(T3(e[0], e[5], e[10]), T3(e[0], e[6], e[9])), T3(e[4], e[1], e[10])), T3(e[4], e[2], e[9])),
+                    T3(e[8], e[1], e[6])), T3(e[8], e[2], e[5]));
+    float det = xa(xa(xa(xm(e[0], inv[0]), xm(e[1], inv[4])), xm(e[2], inv[8])), xm(e[3], inv[12]));
+    float detr = xd(1.0f, det);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) out[i] = xm(inv[i], detr);
+}
+
+__global__ void k_cameras(const float *__restrict__ extr, const float *__restrict__ intr, Camera *__restrict__ cams,
+                          int count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float *e12 = extr + 12 * (size_t)i, *k9 = intr + 9 * (size_t)i;
+    float E[16], K[16], KE[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) E[j] = K[j] = (j % 5 == 0) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        K[4 * r + 0] = k9[3 * r + 0];
+        K[4 * r + 1] = k9[3 * r + 1];
+        K[4 * r + 2] = k9[3 * r + 2];
+        K[4 * r + 3] = 0.0f;
+        E[4 * r + 0] = e12[4 * r + 0];
+        E[4 * r + 1] = e12[4 * r + 1];
+        E[4 * r + 2] = e12[4 * r + 2];
+        E[4 * r + 3] = e12[4 * r + 3];
+    }
+    Camera &cam = cams[i];
+    mat4_inverse_x(E, cam.invE);
+    mat4_mul_x(K, E, KE);
+    mat4_inverse_x(KE, cam.invP);
+    float ow = cam.invE[15];
+    cam.orig[0] = xd(cam.invE[3], ow);
+    cam.orig[1] = xd(cam.invE[7], ow);
+    cam.orig[2] = xd(cam.invE[11], ow);
+    cam.orig[3] = 1.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) cam.origS[j] = xd(cam.orig[j], 1000.0f);
+    cam.origS[3] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 12; ++j) { cam.KE[j] = KE[j]; cam.E[j] = e12[j]; }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) cam.K[j] = k9[j];
+}
+
+// ---------------------------------------------------------------------------- face setup
+
+__global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__restrict__ faces, FaceGeo *__restrict__ geo,
+                           float4 *__restrict__ fnormal, int N, int F, int B) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * F) return;
+    int b = i / F, f = i - b * F;
+    const float *V = verts + (size_t)b * N * 3;
+    int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+    V3 p0 = ld3(V + 3 * i0), p1 = ld3(V + 3 * i1), p2 = ld3(V + 3 * i2);
+    V3 fn = xcross(xsub(p1, p0), xsub(p2, p0));
+    if (fnormal) fnormal[i] = make_float4(fn.x, fn.y, fn.z, 0.0f);
+    // rayTriangleIntersect scales vertices by 1/1000 (RendererUtil.h:29-32)
+    V3 s0 = v3(xd(p0.x, 1000.0f), xd(p0.y, 1000.0f), xd(p0.z, 1000.0f));
+    V3 s1 = v3(xd(p1.x, 1000.0f), xd(p1.y, 1000.0f), xd(p1.z, 1000.0f));
+    V3 s2 = v3(xd(p2.x, 1000.0f), xd(p2.y, 1000.0f), xd(p2.z, 1000.0f));
+    V3 n = xcross(xsub(s1, s0), xsub(s2, s0));
+    FaceGeo g;
+    g.a = make_float4(s0.x, s0.y, s0.z, s1.x);
+    g.b = make_float4(s1.y, s1.z, s2.x, s2.y);
+    g.c = make_float4(s2.z, n.x, n.y, n.z);
+    g.d = make_float4(xdot(s0, n), xdot(n, n), 0.0f, 0.0f);
+    geo[i] = g;
+}
+
+// ---------------------------------------------------------------------------- vertex stage
+
+__global__ void k_vertices(const float *__restrict__ verts, const Topology topo, const float4 *__restrict__ fnormal,
+                           const Camera *__restrict__ cams, float *__restrict__ vnormal_out, float4 *__restrict__ proj,
+                           int B, int C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = topo.N, F = topo.F;
+    if (i >= B * N) return;
+    int b = i / N, v = i - b * N;
+    // vertex normal = sum of adjacent face normals in ascending face order
+    V3 acc = v3(0.0f, 0.0f, 0.0f);
+    int s = topo.vstart[v], e = topo.vstart[v + 1];
+    for (int k = s; k < e; ++k) {
+        float4 n = fnormal[(size_t)b * F + topo.vfaces[k]];
+        if (k == s) acc = v3(n.x, n.y, n.z);
+        else acc = v3(xa(acc.x, n.x), xa(acc.y, n.y), xa(acc.z, n.z));
+    }
+    V3 p = ld3(verts + (size_t)i * 3);
+    for (int c = 0; c < C; ++c) {
+        size_t o = ((size_t)b * C + c) * N + v;
+        float *dst = vnormal_out + o * 3;
+        dst[0] = acc.x;
+        dst[1] = acc.y;
+        dst[2] = acc.z;
+        // getCamSpacePoint + projectPointFloat3 (CameraUtil.h:141-186)
+        const Camera &cam = cams[b * C + c];
+        const float *E = cam.E, *K = cam.K;
+        float cx = xa(xa(xa(xm(E[0], p.x), xm(E[1], p.y)), xm(E[2], p.z)), xm(E[3], 1.0f));
+        float cy = xa(xa(xa(xm(E[4], p.x), xm(E[5], p.y)), xm(E[6], p.z)), xm(E[7], 1.0f));
+        float cz = xa(xa(xa(xm(E[8], p.x), xm(E[9], p.y)), xm(E[10], p.z)), xm(E[11], 1.0f));
+        float x = xa(xa(xm(cx, K[0]), xm(cy, K[1])), xm(cz, K[2]));
+        float y = xa(xa(xm(cx, K[3]), xm(cy, K[4])), xm(cz, K[5]));
+        float z = xa(xa(xm(cx, K[6]), xm(cy, K[7])), xm(cz, K[8]));
+        if (z > 0.0000001f) {
+            x = xd(x, z);
+            y = xd(y, z);
+        } else {
+            z = 0.00001f;
+            x = xd(x, z);
+            y = xd(y, z);
+        }
+        proj[o] = make_float4(x, y, z, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------- binning
+
+__device__ __forceinline__ int4 face_box(float4 p0, float4 p1, float4 p2, int W, int H) {
+    // projectFacesDevice (CUDABasedRasterization.cu:202-206): float boxes
+    // converted to int by truncation.
+    int4 r;
+    r.x = __float2int_rz(fmaxf(xs(fminf(p0.x, fminf(p1.x, p2.x)), 0.5f), 0.0f));
+    r.y = __float2int_rz(fmaxf(xs(fminf(p0.y, fminf(p1.y, p2.y)), 0.5f), 0.0f));
+    r.z = __float2int_rz(fminf(xa(fmaxf(p0.x, fmaxf(p1.x, p2.x)), 0.5f), (float)(W - 1)));
+    r.w = __float2int_rz(fminf(xa(fmaxf(p0.y, fmaxf(p1.y, p2.y)), 0.5f), (float)(H - 1)));
+    return r;
+}
+
+__global__ void k_bin_count(const Topology topo, const float *__restrict__ verts, const float4 *__restrict__ proj,
+                            FrameDims dims, FwdScratch ws) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int F = topo.F, N = topo.N;
+    if (i >= dims.B * dims.C * F) return;
+    int bc = i / F, f = i - bc * F, b = bc / dims.C;
+    const int i0 = topo.faces[3 * f], i1 = topo.faces[3 * f + 1], i2 = topo.faces[3 * f + 2];
+    const float4 *P = proj + (size_t)bc * N;
+    float4 p0 = P[i0], p1 = P[i1], p2 = P[i2];
+    int4 box = face_box(p0, p1, p2, dims.W, dims.H);
+    if (box.x > box.z || box.y > box.w) box = make_int4(1, 1, 0, 0);
+    // screen-space barycentric setup and the error bounds of the skip tests
+    const float ex1 = p1.x - p0.x, ey1 = p1.y - p0.y, ex2 = p2.x - p0.x, ey2 = p2.y - p0.y;
+    const float det = ex1 * ey2 - ey1 * ex2;
+    const float zmn = fminf(p0.z, fminf(p1.z, p2.z)), zmx = fmaxf(p0.z, fmaxf(p1.z, p2.z));
+    const float *V = verts + (size_t)b * N * 3;
+    const Camera &cam = ws.cams[bc];
+    const float4 fn = ws.fnormal[(size_t)b * F + f];
+    const V3 w0 = ld3(V + 3 * i0), w1 = ld3(V + 3 * i1), w2 = ld3(V + 3 * i2);
+    const float cx = (w0.x + w1.x + w2.x) * (1.0f / 3.0f), cy = (w0.y + w1.y + w2.y) * (1.0f / 3.0f),
+                cz = (w0.z + w1.z + w2.z) * (1.0f / 3.0f);
+    const float vx = cx - cam.orig[0], vy = cy - cam.orig[1], vz = cz - cam.orig[2];
+    const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
+    const float fnLen = sqrtf(fn.x * fn.x + fn.y * fn.y + fn.z * fn.z);
+    const float cosv = fabsf(fn.x * vx + fn.y * vy + fn.z * vz) / (fnLen * dist);
+    auto elen = [](V3 a, V3 c) { return sqrtf((a.x - c.x) * (a.x - c.x) + (a.y - c.y) * (a.y - c.y) + (a.z - c.z) * (a.z - c.z)); };
+    const float maxEdge = fmaxf(elen(w0, w1), fmaxf(elen(w1, w2), elen(w2, w0)));
+    const float alt = fnLen / maxEdge;  // smallest altitude, mm
+    const float sEdge = fmaxf(sqrtf(ex1 * ex1 + ey1 * ey1), fmaxf(sqrtf(ex2 * ex2 + ey2 * ey2),
+                              sqrtf((p2.x - p1.x) * (p2.x - p1.x) + (p2.y - p1.y) * (p2.y - p1.y))));
+    const float altPx = fabsf(det) / sEdge;  // smallest screen altitude, pixels
+    const float scale = sqrtf(cam.orig[0] * cam.orig[0] + cam.orig[1] * cam.orig[1] + cam.orig[2] * cam.orig[2]) +
+                        sqrtf(cx * cx + cy * cy + cz * cz) + dist;
+    const bool valid = zmn >= 1.0f && zmx <= 64.0f * zmn && fabsf(det) > 1e-6f && isfinite(det) &&
+                       isfinite(p0.x + p1.x + p2.x + p0.y + p1.y + p2.y) && isfinite(cosv) && alt > 0.0f;
+    int flags = 0;
+    float mIn = 2.0f, mOut = 0.0f, dRel = 1.0f;
+    float4 s1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (valid) {
+        const float zr = zmx / zmn;
+        const float idet = 1.0f / det;
+        s1 = make_float4(ey2 * idet, -ex2 * idet, -ey1 * idet, ex1 * idet);
+        // exact-test barycentric error: hit point off by ~eps*scale/cos along the ray
+        const float eb = (4.0f * 6e-8f * scale / fmaxf(cosv, 1e-6f) + 4.0f * 6e-8f * scale) / alt + 1e-5f;
+        // screen barycentric error: ~3e-4 px of projection and ray-direction error
+        const float es = 3e-4f / altPx + 1e-6f;
+        mIn = (2.0f * (eb + es) + 1e-4f) * zr;
+        mOut = mIn + 2e-3f * zr;
+        dRel = 2.0f * (eb + es) * (zr - 1.0f) + 1e-4f;
+        // certainly accepted needs |N.d| (scaled units) clear of the 1e-7 parallel test
+        const bool clear = fnLen * 1e-6f * cosv >= 4e-7f;
+        flags = kScreenValid | ((cosv >= 0.02f && clear && mIn < 0.2f) ? kCertain : 0);
+    }
+    ViewFace vf;
+    vf.hdr = make_int4(box.x | (box.z << 16), box.y | (box.w << 16), flags, __float_as_int(dRel));
+    vf.z = make_float4(p0.z, p1.z, p2.z, mIn);
+    vf.s0 = make_float4(p0.x, p0.y, mOut, zmn * (10000.0f / 1.0025f) - 2.0f);
+    vf.s1 = s1;
+    ws.vface[i] = vf;
+    if (box.x > box.z || box.y > box.w) return;
+    int tx0 = box.x / kTile, tx1 = box.z / kTile, ty0 = box.y / kTile, ty1 = box.w / kTile;
+    int nt = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+    const int T = dims.tilesX * dims.tilesY;
+    if (nt > kBigTiles) {
+        int k = atomicAdd(&ws.bigCount[bc], 1);
+        ws.bigList[(size_t)bc * F + k] = f;
+        return;
+    }
+    int *cnt = ws.tileCount + (size_t)bc * T;
+    for (int ty = ty0; ty <= ty1; ++ty)
+        for (int tx = tx0; tx <= tx1; ++tx) atomicAdd(&cnt[ty * dims.tilesX + tx], 1);
+}
+
+// Exclusive scan of n counts by one 1024-thread block.
+__global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ count, int *__restrict__ start, int n) {
+    __shared__ int warpSum[32];
+    __shared__ int carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 1024) {
+        int idx = base + tid;
+        int x = idx < n ? count[idx] : 0;
+        int incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warpSum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int w = warpSum[lane];
+            int wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            warpSum[lane] = wi - w;  // exclusive prefix of warp sums
+        }
+        __syncthreads();
+        int excl = carry + warpSum[warp] + incl - x;
+        if (idx < n) start[idx] = excl;
+        __syncthreads();
+        if (tid == 1023) carry = excl + x;
+        __syncthreads();
+    }
+    if (tid == 0) start[n] = carry;
+}
+
+__global__ void k_bin_fill(const Topology topo, FrameDims dims, FwdScratch ws) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int F = topo.F;
+    if (i >= dims.B * dims.C * F) return;
+    int bc = i / F, f = i - bc * F;
+    int4 box = vf_box(ws.vface[i]);
+    if (box.x > box.z || box.y > box.w) return;
+    int tx0 = box.x / kTile, tx1 = box.z / kTile, ty0 = box.y / kTile, ty1 = box.w / kTile;
+    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > kBigTiles) return;
+    const int T = dims.tilesX * dims.tilesY;
+    for (int ty = ty0; ty <= ty1; ++ty)
+        for (int tx = tx0; tx <= tx1; ++tx) {
+            size_t t = (size_t)bc * T + ty * dims.tilesX + tx;
+            int pos = atomicAdd(&ws.tileCursor[t], 1);
+            ws.bins[ws.tileStart[t] + pos] = f;
+        }
+}
+
+// ---------------------------------------------------------------------------- host launch
+
+static inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
+
+cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, int count, cudaStream_t st) {
+    GVR_LAUNCH(st, "k_cameras", k_cameras<<<blocks(count, 64), 64, 0, st>>>(extr, intr, cams, count));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *geo, float4 *fnormal, int B,
+                            cudaStream_t st) {
+    GVR_LAUNCH(st, "k_face_geo",
+               k_face_geo<<<blocks((size_t)B * topo.F, 256), 256, 0, st>>>(verts, topo.faces, geo, fnormal, topo.N,
+                                                                            topo.F, B));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forward(const Topology &topo, const FrameDims &dims, const FwdScratch &ws, const float *verts,
+                           const float *colors, const float *texture, const float *sh, const float *extr,
+                           const float *intr, float *bary, int32_t *face, float *render, float *vnormal,
+                           float4 *proj, cudaStream_t st) {
+    const int B = dims.B, C = dims.C, T = dims.tilesX * dims.tilesY;
+    cudaError_t err = cudaMemsetAsync(ws.zeroBase, 0, ws.zeroBytes, st);
+    if (err != cudaSuccess) return err;
+    if ((err = launch_cameras(extr, intr, ws.cams, B * C, st)) != cudaSuccess) return err;
+    if ((err = launch_face_geo(verts, topo, ws.geo, ws.fnormal, B, st)) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_vertices",
+               k_vertices<<<blocks((size_t)B * topo.N, 256), 256, 0, st>>>(verts, topo, ws.fnormal, ws.cams, vnormal,
+                                                                            proj, B, C));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    const size_t nvf = (size_t)B * C * topo.F;
+    GVR_LAUNCH(st, "k_bin_count", k_bin_count<<<blocks(nvf, 256), 256, 0, st>>>(topo, verts, proj, dims, ws));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_scan_tiles", k_scan_tiles<<<1, 1024, 0, st>>>(ws.tileCount, ws.tileStart, B * C * T));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_bin_fill", k_bin_fill<<<blocks(nvf, 256), 256, 0, st>>>(topo, dims, ws));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    RasterIO io{verts, colors, texture, sh, vnormal, bary, face, render};
+    return launch_raster(topo, dims, ws, io, st);
+}
+
+// Per-pixel rays for tests (same pixel_ray as the raster).
+__global__ void k_debug_rays(const Camera *__restrict__ cams, float *__restrict__ out, int BC, int W, int H) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)BC * W * H) return;
+    int u = (int)(i % W);
+    int v = (int)((i / W) % H);
+    int bc = (int)(i / ((size_t)W * H));
+    V3 d = pixel_ray(cams[bc], u, v);
+    out[3 * i + 0] = d.x;
+    out[3 * i + 1] = d.y;
+    out[3 * i + 2] = d.z;
+}
+
+cudaError_t launch_debug_rays(const Camera *cams, float *out, int BC, int W, int H, cudaStream_t st) {
+    GVR_LAUNCH(st, "k_debug_rays", k_debug_rays<<<blocks((size_t)BC * W * H, 256), 256, 0, st>>>(cams, out, BC, W, H));
+    return cudaGetLastError();
+}
+
+}  // namespace gvr

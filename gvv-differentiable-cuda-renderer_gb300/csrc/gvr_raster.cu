@@ -1,0 +1,296 @@
+// gvr_raster.cu -- visibility, resolve and shading of one 16x16 pixel tile
+// per block (the work of renderDepthBufferDevice + renderBuffersDevice,
+// cpp/src/Renderer/CUDABasedRasterization.cu:215-408).
+//
+// The reference tests every pixel of every face's box with its FP32
+// world-space ray/triangle test and keeps the smallest quantised depth.
+// Here each thread owns one pixel and the warps walk the tile's face
+// entries (staged in shared memory) twice with cheap screen-space bounds:
+//
+//   A  faces that certainly cover the pixel lower its depth bound zup
+//      (the face's exact quantised depth is <= zup);
+//   B  faces that may still win the pixel (not certainly outside, and not
+//      certainly deeper than zup + 2 units) become its candidates;
+//
+// then the resolve runs the reference's exact test on the candidates only
+// and keeps the packed depth|face minimum.  Every skipped face provably has
+// a larger quantised depth than a face the exact test accepts, so the face
+// ids and barycentrics equal those of testing every face (ties between
+// equal depths go to the smallest face id; the reference resolves them by a
+// write race).
+#include "gvr_internal.cuh"
+#include "gvr_kernels.h"
+#include "gvr_profile.h"
+
+namespace gvr {
+namespace {
+
+constexpr int kCachedEntries = 512;  // compacted face entries of a tile kept in shared memory
+constexpr int kMaxCand = 4;          // candidates a pixel keeps in registers
+
+// Face entry with its skip-test constants and its box clipped to the tile (80 bytes).
+struct __align__(16) Entry {
+    float x0, y0, a1, b1;
+    float a2, b2, r0, r1;
+    float r2, mIn, mOut, dRel;
+    float zLowSafe;
+    int flags, f, pad;
+    int bx0, by0, bx1, by1;
+};
+
+__device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX0, int tileY0) {
+    Entry E;
+    E.x0 = vf.s0.x;
+    E.y0 = vf.s0.y;
+    E.a1 = vf.s1.x;
+    E.b1 = vf.s1.y;
+    E.a2 = vf.s1.z;
+    E.b2 = vf.s1.w;
+    E.r0 = __frcp_rn(vf.z.x);
+    E.r1 = __frcp_rn(vf.z.y);
+    E.r2 = __frcp_rn(vf.z.z);
+    E.mIn = vf.z.w;
+    E.mOut = vf.s0.z;
+    E.dRel = vf_drel(vf);
+    E.zLowSafe = vf.s0.w;
+    E.flags = vf_flags(vf);
+    E.f = f;
+    E.pad = 0;
+    const int4 box = vf_box(vf);
+    E.bx0 = max(box.x, tileX0);
+    E.by0 = max(box.y, tileY0);
+    E.bx1 = min(box.z, tileX0 + kTile - 1);
+    E.by1 = min(box.w, tileY0 + kTile - 1);
+    return E;
+}
+
+// Screen barycentrics of pixel centre (px, py) and the depth estimate 1e4*S/T
+// (the reference's 1e4 / sum(b_i / z_i) with b_i its world barycentrics).
+__device__ __forceinline__ void entry_lambda(const Entry &E, float px, float py, float &l0, float &l1, float &l2) {
+    const float dx = px - E.x0, dy = py - E.y0;
+    l1 = E.a1 * dx + E.b1 * dy;
+    l2 = E.a2 * dx + E.b2 * dy;
+    l0 = 1.0f - l1 - l2;
+}
+
+__device__ __forceinline__ float entry_depth(const Entry &E, float l0, float l1, float l2) {
+    const float S = l0 * E.r0 + l1 * E.r1 + l2 * E.r2;
+    const float T = l0 * E.r0 * E.r0 + l1 * E.r1 * E.r1 + l2 * E.r2 * E.r2;
+    return 10000.0f * __fdividef(S, T);
+}
+
+// Pass A test: depth upper bound if the face certainly covers the pixel, else +inf.
+__device__ __forceinline__ float certain_zup(const Entry &E, float px, float py) {
+    float l0, l1, l2;
+    entry_lambda(E, px, py, l0, l1, l2);
+    if (l0 >= E.mIn && l1 >= E.mIn && l2 >= E.mIn) return entry_depth(E, l0, l1, l2) * (1.0f + E.dRel) + 2.0f;
+    return __int_as_float(0x7f800000);
+}
+
+// Pass B test: may the face win the pixel against the certain bound zup?
+__device__ __forceinline__ bool may_win(const Entry &E, float px, float py, float zup) {
+    if (!(E.flags & kScreenValid)) return true;
+    float l0, l1, l2;
+    entry_lambda(E, px, py, l0, l1, l2);
+    if (l0 < -E.mOut || l1 < -E.mOut || l2 < -E.mOut) return false;  // certainly outside
+    float zlow = E.zLowSafe;  // lower bound of its quantised depth if accepted
+    if (E.dRel < 0.25f) zlow = fmaxf(zlow, entry_depth(E, l0, l1, l2) * (1.0f - E.dRel) - 2.0f);
+    return !(zlow > zup);
+}
+
+struct ExactCtx {
+    const FaceGeo *geo;      // [F] of this batch element
+    const ViewFace *vface;   // [F] of this view
+    V3 origS;
+    V3 d;
+};
+
+// The reference's exact test of face f at this pixel; key = kEmptyKey if rejected.
+__device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f, V3 &abc) {
+    const FaceSetup fs = load_face(&x.geo[f]);
+    abc = barycentric(fs, x.origS, xdot(x.origS, fs.n), x.d);
+    if (!inside(abc)) return kEmptyKey;
+    const float4 z = x.vface[f].z;
+    return depth_key(depth_quantised(abc, z.x, z.y, z.z), f);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameDims dims, FwdScratch ws, RasterIO io) {
+    __shared__ Entry sE[kCachedEntries];
+    __shared__ int sCount;
+    const int T = dims.tilesX * dims.tilesY;
+    const int tile = blockIdx.x % T, bc = blockIdx.x / T, b = bc / dims.C;
+    const int tileX0 = (tile % dims.tilesX) * kTile, tileY0 = (tile / dims.tilesX) * kTile;
+    const int tid = threadIdx.x;
+    const int u = tileX0 + (tid & (kTile - 1)), v = tileY0 + tid / kTile;
+    const float px = u + 0.5f, py = v + 0.5f;
+    const int F = topo.F;
+    const ViewFace *VF = ws.vface + (size_t)bc * F;
+    const int *bigList = ws.bigList + (size_t)bc * F;
+    const size_t tIdx = (size_t)bc * T + tile;
+    const int s0 = ws.tileStart[tIdx], nTile = ws.tileStart[tIdx + 1] - s0;
+    const int nAll = nTile + ws.bigCount[bc];
+
+    // stage the entries whose box meets the tile (compacted; order does not matter)
+    if (tid == 0) sCount = 0;
+    __syncthreads();
+    for (int e = tid; e < nAll; e += kTilePix) {
+        const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
+        const Entry E = make_entry(VF[f], f, tileX0, tileY0);
+        if (E.bx0 > E.bx1 || E.by0 > E.by1) continue;
+        const int slot = atomicAdd(&sCount, 1);
+        if (slot < kCachedEntries) sE[slot] = E;
+    }
+    __syncthreads();
+    const int nE = sCount;
+    const bool overflow = nE > kCachedEntries;  // block-uniform: then walk the global list instead
+    const int rowLo = tileY0 + 2 * (tid >> 5), rowHi = rowLo + 1;  // the two rows of this warp
+
+    auto entry_at = [&](int e, Entry &E) -> bool {
+        if (!overflow) {
+            E = sE[e];
+            return true;
+        }
+        const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
+        E = make_entry(VF[f], f, tileX0, tileY0);
+        return E.bx0 <= E.bx1 && E.by0 <= E.by1;
+    };
+    const int nWalk = overflow ? nAll : nE;
+
+    // pass A: certain depth bound
+    float zup = __int_as_float(0x7f800000);
+    for (int e = 0; e < nWalk; ++e) {
+        Entry E;
+        if (!entry_at(e, E)) continue;
+        if (!(E.flags & kCertain) || E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
+        if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
+        zup = fminf(zup, certain_zup(E, px, py));
+    }
+
+    // pass B: candidates (the last kMaxCand are kept; more means the slow path)
+    int cnt = 0, c0 = -1, c1 = -1, c2 = -1, c3 = -1;
+    for (int e = 0; e < nWalk; ++e) {
+        Entry E;
+        if (!entry_at(e, E)) continue;
+        if (E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
+        if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
+        if (may_win(E, px, py, zup)) {
+            c3 = c2;
+            c2 = c1;
+            c1 = c0;
+            c0 = E.f;
+            ++cnt;
+        }
+    }
+
+    if (u >= dims.W || v >= dims.H) return;
+
+    // resolve: the reference's exact test on the candidates
+    const Camera &cam = ws.cams[bc];
+    ExactCtx x;
+    x.geo = ws.geo + (size_t)b * F;
+    x.vface = VF;
+    x.origS = v3(cam.origS[0], cam.origS[1], cam.origS[2]);
+    x.d = pixel_ray(cam, u, v);
+    unsigned long long best = kEmptyKey;
+    V3 abc = v3(0.0f, 0.0f, 0.0f);
+    if (cnt <= kMaxCand) {
+        const int cs[kMaxCand] = {c0, c1, c2, c3};
+#pragma unroll
+        for (int i = 0; i < kMaxCand; ++i) {
+            if (i >= cnt) break;
+            V3 t;
+            const unsigned long long k = exact_key(x, cs[i], t);
+            if (k < best) {
+                best = k;
+                abc = t;
+            }
+        }
+    } else {
+        for (int e = 0; e < nWalk; ++e) {
+            Entry E;
+            if (!entry_at(e, E)) continue;
+            if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
+            if (!may_win(E, px, py, zup)) continue;
+            V3 t;
+            const unsigned long long k = exact_key(x, E.f, t);
+            if (k < best) {
+                best = k;
+                abc = t;
+            }
+        }
+    }
+
+    const size_t p = ((size_t)bc * dims.H + v) * dims.W + u;
+    if (best == kEmptyKey) {
+        io.face[p] = -1;
+        reinterpret_cast<float2 *>(io.bary)[p] = make_float2(0.0f, 0.0f);
+        io.render[3 * p + 0] = 0.0f;
+        io.render[3 * p + 1] = 1.0f;
+        io.render[3 * p + 2] = 0.0f;
+        return;
+    }
+    const int f = (int)(unsigned)(best & 0xffffffffull);
+    const int i0 = topo.faces[3 * f], i1 = topo.faces[3 * f + 1], i2 = topo.faces[3 * f + 2];
+    io.face[p] = f;
+    reinterpret_cast<float2 *>(io.bary)[p] = make_float2(abc.x, abc.y);
+
+    // shading (CUDABasedRasterization.cu:307-403)
+    const V3 d = x.d;
+    const float *VN = io.vnormal + (size_t)bc * topo.N * 3;
+    V3 un = pixel_normal_un(ld3(VN + 3 * i0), ld3(VN + 3 * i1), ld3(VN + 3 * i2), abc);
+    float len = __fsqrt_rn(xdot(un, un));
+    V3 n = v3(xd(un.x, len), xd(un.y, len), xd(un.z, len));
+    if (xdot(n, d) > 0.0f) n = v3(-n.x, -n.y, -n.z);
+    float3 col;
+    switch (dims.albedo) {
+        case GVR_ALBEDO_TEXTURED: {
+            float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+            int LU = __float2int_rz(xs(tc.x, 0.5f)), LV = __float2int_rz(xs(tc.y, 0.5f));
+            const float *t = io.texture + (((size_t)b * dims.Ht + LV) * dims.Wt + LU) * 3;
+            col = make_float3(t[0], t[1], t[2]);
+            break;
+        }
+        case GVR_ALBEDO_VERTEX_COLOR: {
+            const float *Cb = io.colors + (size_t)b * topo.N * 3;
+            const float *q0 = Cb + 3 * i0, *q1 = Cb + 3 * i1, *q2 = Cb + 3 * i2;
+            col = make_float3(q0[0] * abc.x + q1[0] * abc.y + q2[0] * abc.z, q0[1] * abc.x + q1[1] * abc.y + q2[1] * abc.z,
+                              q0[2] * abc.x + q1[2] * abc.y + q2[2] * abc.z);
+            break;
+        }
+        case GVR_ALBEDO_NORMAL:
+            col = make_float3((1.0f + n.x) * 0.5f, (1.0f + n.y) * 0.5f, (1.0f + n.z) * 0.5f);
+            break;
+        default:
+            col = make_float3(1.0f, 1.0f, 1.0f);
+            break;
+    }
+    const bool shaded = (dims.shading == GVR_SHADING_SHADED && dims.albedo != GVR_ALBEDO_NORMAL) ||
+                        dims.albedo == GVR_ALBEDO_LIGHTING;
+    if (shaded) {
+        const float *sh = io.sh + (size_t)bc * 27;
+        float basis[9];
+        sh_basis(n, basis);
+        float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            l0 += sh[k] * basis[k];
+            l1 += sh[9 + k] * basis[k];
+            l2 += sh[18 + k] * basis[k];
+        }
+        col = make_float3(col.x * l0, col.y * l1, col.z * l2);
+    }
+    io.render[3 * p + 0] = col.x;
+    io.render[3 * p + 1] = col.y;
+    io.render[3 * p + 2] = col.z;
+}
+
+cudaError_t launch_raster(const Topology &topo, const FrameDims &dims, const FwdScratch &ws, const RasterIO &io,
+                          cudaStream_t st) {
+    const int grid = dims.B * dims.C * dims.tilesX * dims.tilesY;
+    GVR_LAUNCH(st, "k_raster", k_raster<<<grid, kTilePix, 0, st>>>(topo, dims, ws, io));
+    return cudaGetLastError();
+}
+
+}  // namespace gvr

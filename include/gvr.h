@@ -1,0 +1,183 @@
+/*
+ * gvr.h -- C ABI of the GB300 differentiable mesh rasteriser.
+ *
+ * Drop-in boundary for the reference's CudaRenderer operator pair:
+ *   gvr_create   <- CudaRenderer / CudaRendererGrad op construction
+ *                   (cpp/src/TensorflowOperators/CudaRenderer/CudaRenderer.cpp:37-155,
+ *                    CudaRendererGrad.cpp:43-101) and the renderer constructors
+ *                   (cpp/src/Renderer/CUDABasedRasterization.cpp:11-106,
+ *                    CUDABasedRasterizationGrad.cpp:7-87): attrs, topology,
+ *                   vertex->face adjacency.
+ *   gvr_forward  <- CudaRenderer::Compute (CudaRenderer.cpp:298-335) and the op
+ *                   signature REGISTER_OP("CudaRendererGpu") (CudaRenderer.cpp:5-33).
+ *   gvr_backward <- CudaRendererGrad::Compute (CudaRendererGrad.cpp:252-293) and
+ *                   REGISTER_OP("CudaRendererGradGpu") (CudaRendererGrad.cpp:6-39).
+ *   gvr_destroy  <- the renderer destructors (CUDABasedRasterization.cpp:110-121).
+ *
+ * Conventions: every tensor pointer is a device pointer to C-contiguous
+ * float32 (int32 for faces) data in the reference's layouts; `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Calls return a GvrStatus and
+ * never abort; gvr_last_error() gives the calling thread's last message.
+ * A handle is immutable after gvr_create and may be used from several
+ * streams at once; per-call scratch is either the caller's workspace or
+ * stream-ordered memory (cudaMallocAsync) owned by the call.
+ */
+#ifndef GVR_H
+#define GVR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GVR_ABI_VERSION 1
+
+typedef enum {
+    GVR_OK = 0,
+    GVR_ERR_INVALID_ARGUMENT = -1, /* bad size, pointer, index or mode             */
+    GVR_ERR_CUDA = -2,             /* a CUDA runtime call or kernel launch failed  */
+    GVR_ERR_OUT_OF_MEMORY = -3,    /* device allocation failed                     */
+    GVR_ERR_WORKSPACE = -4,        /* caller workspace smaller than required       */
+    GVR_ERR_UNSUPPORTED = -5       /* combination not supported by this build      */
+} GvrStatus;
+
+/* AlbedoMode / ShadingMode (cpp/src/Renderer/CUDABasedRasterizationInput.h:25-35). */
+typedef enum {
+    GVR_ALBEDO_VERTEX_COLOR = 0,
+    GVR_ALBEDO_TEXTURED = 1,
+    GVR_ALBEDO_NORMAL = 2,
+    GVR_ALBEDO_LIGHTING = 3,
+    GVR_ALBEDO_FOREGROUND_MASK = 4
+} GvrAlbedoMode;
+
+typedef enum { GVR_SHADING_SHADED = 0, GVR_SHADING_SHADELESS = 1 } GvrShadingMode;
+
+typedef struct GvrHandle GvrHandle;
+
+/* Op attrs `faces`, `texture_coordinates`, `number_of_vertices`
+ * (CudaRenderer.cpp:23-25); host pointers, copied by gvr_create. */
+typedef struct {
+    const int32_t *faces;              /* [F*3] vertex ids                     */
+    const float *texture_coordinates;  /* [F*6] per-corner (u, v); may be NULL */
+    int32_t num_faces;                 /* F                                    */
+    int32_t num_vertices;              /* N                                    */
+} GvrTopology;
+
+/* Remaining op attrs (CudaRenderer.cpp:26-33). */
+typedef struct {
+    int32_t num_cameras;          /* number_of_cameras                         */
+    int32_t render_resolution_u;  /* W                                         */
+    int32_t render_resolution_v;  /* H                                         */
+    int32_t albedo_mode;          /* GvrAlbedoMode                             */
+    int32_t shading_mode;         /* GvrShadingMode (foregroundMask forces shadeless) */
+    int32_t image_filter_size;    /* >= 1, window half-size of the target-image gradient */
+    int32_t texture_filter_size;  /* >= 1, accepted; unused by the reference kernels too */
+    int32_t compute_normal_map;   /* 0/1 */
+} GvrAttrs;
+
+/* CudaRendererGpu inputs 0-6 and outputs 0-5 (CudaRenderer.cpp:7-20). */
+typedef struct {
+    int32_t batch;                /* B                                          */
+    int32_t texture_height;       /* Ht (texture dim 1)                         */
+    int32_t texture_width;        /* Wt (texture dim 2)                         */
+    const float *vertex_pos;      /* [B,N,3]                                    */
+    const float *vertex_color;    /* [B,N,3]                                    */
+    const float *texture;         /* [B,Ht,Wt,3]                                */
+    const float *sh_coeff;        /* [B,C,27]                                   */
+    const float *target_image;    /* [B,C,H,W,3]; read only for target_image_out */
+    const float *extrinsics;      /* [B,C,12] world->camera 3x4 row-major       */
+    const float *intrinsics;      /* [B,C,9] 3x3 row-major                      */
+    float *barycentric;           /* out [B,C,H,W,2]                            */
+    int32_t *face;                /* out [B,C,H,W], -1 = background             */
+    float *render;                /* out [B,C,H,W,3]                            */
+    float *vertex_normal;         /* out [B,C,N,3]                              */
+    float *target_image_out;      /* out [B,C,H,W,3] copy of target_image, or NULL */
+    float *normal_map;            /* out [B,Ht,Wt,3] (compute_normal_map), or NULL */
+    void *workspace;              /* optional device scratch, >= gvr_forward_workspace_size */
+    size_t workspace_bytes;
+} GvrForwardArgs;
+
+/* CudaRendererGradGpu inputs 0-11 and outputs 0-3 (CudaRendererGrad.cpp:8-29). */
+typedef struct {
+    int32_t batch;
+    int32_t texture_height;
+    int32_t texture_width;
+    const float *render_grad;     /* [B,C,H,W,3]                                */
+    const float *vertex_pos;      /* [B,N,3]                                    */
+    const float *vertex_color;    /* [B,N,3]                                    */
+    const float *texture;         /* [B,Ht,Wt,3]                                */
+    const float *sh_coeff;        /* [B,C,27]                                   */
+    const float *target_image;    /* [B,C,H,W,3]; may be NULL if target_grad is NULL */
+    const float *vertex_normal;   /* [B,C,N,3] (forward output)                 */
+    const float *barycentric;     /* [B,C,H,W,2] accepted; barycentrics are recomputed from `face` */
+    const int32_t *face;          /* [B,C,H,W] (forward output)                 */
+    const float *target_grad;     /* [B,C,H,W,3] upstream grad of target_image_out, or NULL = 0 */
+    const float *extrinsics;      /* [B,C,12]                                   */
+    const float *intrinsics;      /* [B,C,9]                                    */
+    float *vertex_pos_grad;       /* out [B,N,3]                                */
+    float *vertex_color_grad;     /* out [B,N,3]                                */
+    float *texture_grad;          /* out [B,Ht,Wt,3]                            */
+    float *sh_coeff_grad;         /* out [B,C,27]                               */
+    void *workspace;
+    size_t workspace_bytes;
+} GvrBackwardArgs;
+
+/* Builds the device topology and vertex->face adjacency in O(F)
+ * (replaces the O(N*F) getVertexFaces, CUDABasedRasterization.cpp:125-154).
+ * Uses the current CUDA device. */
+int gvr_create(const GvrTopology *topology, const GvrAttrs *attrs, GvrHandle **out_handle);
+
+/* Frees everything the handle owns (and nothing else). NULL is a no-op. */
+void gvr_destroy(GvrHandle *handle);
+
+/* Forward render of all B x C views (CUDABasedRasterization.cu:449-473). */
+int gvr_forward(GvrHandle *handle, const GvrForwardArgs *args, void *stream);
+
+/* Gradients (CUDABasedRasterizationGrad.cu:624-635).  For albedo modes
+ * normal/lighting it writes zeros, as python/CudaRenderer.py:207-213 returns. */
+int gvr_backward(GvrHandle *handle, const GvrBackwardArgs *args, void *stream);
+
+/* Device scratch a call needs for the given batch and texture size. */
+size_t gvr_forward_workspace_size(const GvrHandle *handle, int32_t batch, int32_t texture_height,
+                                  int32_t texture_width);
+size_t gvr_backward_workspace_size(const GvrHandle *handle, int32_t batch, int32_t texture_height,
+                                   int32_t texture_width);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *gvr_last_error(void);
+
+/* GVR_ABI_VERSION of the loaded library. */
+int gvr_abi_version(void);
+
+/* Test hook with no reference counterpart: the per-pixel FP32 ray directions
+ * [B,C,H,W,3] exactly as the raster and backward kernels compute them
+ * (getRayCuda2, cpp/src/Utils/CameraUtil.h:251-257). */
+int gvr_debug_rays(GvrHandle *handle, int32_t batch, const float *extrinsics, const float *intrinsics,
+                   float *rays_out, void *stream);
+
+/* Per-kernel timing, no reference counterpart.  While enabled, every kernel
+ * the library launches is bracketed by a CUDA event pair on its stream;
+ * gvr_profile_read waits for those events and reports, per kernel name, the
+ * launches and summed milliseconds since the last gvr_profile_enable call. */
+typedef struct {
+    char name[48];
+    long long launches;
+    double total_ms;
+} GvrKernelTime;
+
+/* Turns timing on (1) or off (0), clears the tallies; returns the previous state. */
+int gvr_profile_enable(int enable);
+
+/* Fills up to `capacity` entries; returns the number of distinct kernels timed. */
+int gvr_profile_read(GvrKernelTime *out, int capacity);
+
+/* Kernels launched by this library since it was loaded (profiling on or off). */
+long long gvr_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GVR_H */

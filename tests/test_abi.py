@@ -1,0 +1,89 @@
+"""C-ABI checks that need no GPU: libgvr.so builds, loads, exports every
+symbol include/gvr.h declares, and rejects bad arguments with a status code
+(validation runs on the host before any CUDA call)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "gvr.h")
+
+
+def _declared():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|long long|const char \*)\s*\*?\s*(gvr_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from gvr import _lib
+    return _lib.load()
+
+
+def test_header_symbols_exported(lib):
+    from gvr import _lib
+    names = _declared()
+    assert len(names) >= 8
+    assert set(names) == set(_lib.EXPORTS)
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_abi_version(lib):
+    src = open(HEADER).read()
+    v = int(re.search(r"#define GVR_ABI_VERSION (\d+)", src).group(1))
+    assert lib.gvr_abi_version() == v
+
+
+def _create(lib, faces, N, C=1, W=8, H=8, albedo=0, shading=0, img_filter=1, tex_filter=1, nmap=0, uvs=None):
+    from gvr import _lib
+    f = np.ascontiguousarray(faces, np.int32).reshape(-1)
+    t = None if uvs is None else np.ascontiguousarray(uvs, np.float32)
+    topo = _lib.GvrTopology(f.ctypes.data, None if t is None else t.ctypes.data, f.size // 3, N)
+    attrs = _lib.GvrAttrs(C, W, H, albedo, shading, img_filter, tex_filter, nmap)
+    h = ctypes.c_void_p()
+    rc = lib.gvr_create(ctypes.byref(topo), ctypes.byref(attrs), ctypes.byref(h))
+    return rc, h, lib.gvr_last_error().decode()
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(N=0), "number_of_vertices"),
+    (dict(C=0), "number_of_cameras"),
+    (dict(W=0), "render_resolution_u"),
+    (dict(H=0), "render_resolution_v"),
+    (dict(albedo=7), "ALBEDO"),
+    (dict(shading=3), "SHADING"),
+    (dict(img_filter=0), "IMAGE FILTER"),
+    (dict(tex_filter=0), "TEXTURE FILTER"),
+])
+def test_create_rejects_bad_attrs(lib, kw, msg):
+    args = dict(faces=[0, 1, 2], N=3)
+    args.update(kw)
+    rc, h, err = _create(lib, **args)
+    assert rc == -1 and not h.value and msg in err
+
+
+def test_create_rejects_out_of_range_face(lib):
+    rc, h, err = _create(lib, [0, 1, 5], 3)
+    assert rc == -1 and "outside" in err
+
+
+def test_calls_reject_null(lib):
+    from gvr import _lib
+    assert lib.gvr_forward(None, None, None) == -1
+    assert lib.gvr_backward(None, None, None) == -1
+    assert lib.gvr_forward_workspace_size(None, 1, 1, 1) == 0
+    lib.gvr_destroy(None)  # no-op
+    assert lib.gvr_debug_rays(None, 1, None, None, None, None) == -1
+    assert "bad" in lib.gvr_last_error().decode()
+
+
+def test_error_status_raises(lib):
+    from gvr import _lib
+    with pytest.raises(_lib.GvrError) as ei:
+        _lib.check(lib.gvr_forward(None, None, None))
+    assert ei.value.status == -1

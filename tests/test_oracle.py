@@ -1,0 +1,252 @@
+"""CPU checks of the oracle (the CPU restatement of the reference kernels).
+
+The reference ships no tests or golden vectors for this path, so the oracle
+is pinned three ways here: (1) FP32 pieces re-derived independently in numpy
+with one IEEE operation per step (numpy float32 arithmetic never contracts),
+(2) finite differences of an FP64 render at fixed visibility for every
+gradient the reference computes as a true derivative, and (3) the committed
+fixtures produced by the reference's own kernels (tests/test_golden.py).
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_scene, rel_norm, small_scene
+from oracle import oracle as orc
+
+f32 = np.float32
+
+
+def _np_project(extr, intr, verts):
+    """getCamSpacePoint + projectPointFloat3 (cpp/src/Utils/CameraUtil.h:141-186) in numpy float32."""
+    E = extr.reshape(3, 4).astype(f32)
+    K = intr.reshape(3, 3).astype(f32)
+    v = verts.astype(f32)
+    cam = [((E[r, 0] * v[:, 0] + E[r, 1] * v[:, 1]) + E[r, 2] * v[:, 2]) + E[r, 3] * f32(1) for r in range(3)]
+    out = []
+    for r in range(3):
+        out.append((cam[0] * K[r, 0] + cam[1] * K[r, 1]) + cam[2] * K[r, 2])
+    x, y, z = out
+    ok = z > f32(1e-7)
+    z = np.where(ok, z, f32(1e-5)).astype(f32)
+    return np.stack([x / z, y / z, z], 1).astype(f32)
+
+
+def _trunc_sat(x):
+    x = np.asarray(x, np.float64)
+    r = np.where(np.isnan(x), 0, np.clip(np.trunc(x), -2147483648.0, 2147483647.0))
+    return r.astype(np.int64).astype(np.int32)
+
+
+def test_camera_inverse_matches_fp64():
+    s = small_scene(views=4)
+    for c in range(4):
+        invE, invP = orc.camera_inverse(s["extrinsics"][0, c], s["intrinsics"][0, c])
+        E = np.eye(4)
+        E[:3] = s["extrinsics"][0, c].reshape(3, 4)
+        K = np.eye(4)
+        K[:3, :3] = s["intrinsics"][0, c].reshape(3, 3)
+        # FP32 cofactor inverses: products with the matrices are the identity to FP32 rounding
+        # (the translation column is ~3000 mm, so its FP32 residual is ~1e-4 mm)
+        assert np.abs(invE.astype(np.float64) @ E - np.eye(4))[:, :3].max() < 1e-6
+        assert np.abs(invE.astype(np.float64) @ E - np.eye(4)).max() < 1e-3
+        assert np.abs(invP.astype(np.float64) @ (K @ E) - np.eye(4)).max() < 1e-3
+
+
+def test_projection_and_boxes_bit_exact_vs_numpy():
+    s = small_scene(views=3, size=96)
+    o = oracle_scene(s)
+    for c in range(3):
+        proj, box = o.project(c)
+        ref = _np_project(s["extrinsics"][0, c], s["intrinsics"][0, c], s["vertex_pos"][0])
+        assert np.array_equal(proj.view(np.uint32), ref.view(np.uint32))
+        p = ref[s["faces"]]
+        W = H = 96
+        x0 = _trunc_sat(np.maximum(p[:, :, 0].min(1) - f32(0.5), f32(0)))
+        y0 = _trunc_sat(np.maximum(p[:, :, 1].min(1) - f32(0.5), f32(0)))
+        x1 = _trunc_sat(np.minimum(p[:, :, 0].max(1) + f32(0.5), f32(W - 1)))
+        y1 = _trunc_sat(np.minimum(p[:, :, 1].max(1) + f32(0.5), f32(H - 1)))
+        assert np.array_equal(box, np.stack([x0, y0, x1, y1], 1))
+
+
+def test_vertex_normals_bit_exact_vs_numpy():
+    s = small_scene()
+    out = oracle_scene(s).forward()
+    v = s["vertex_pos"][0].astype(f32)
+    F = s["faces"]
+    a, b = v[F[:, 1]] - v[F[:, 0]], v[F[:, 2]] - v[F[:, 0]]
+    fn = np.stack([a[:, 1] * b[:, 2] - a[:, 2] * b[:, 1], a[:, 2] * b[:, 0] - a[:, 0] * b[:, 2],
+                   a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]], 1).astype(f32)
+    vn = np.zeros_like(v)
+    first = np.ones(len(v), bool)
+    for f in range(len(F)):                     # ascending face order, first assigned then added
+        for vid in dict.fromkeys(F[f].tolist()):
+            vn[vid] = fn[f] if first[vid] else (vn[vid] + fn[f]).astype(f32)
+            first[vid] = False
+    for c in range(out["vertex_normal"].shape[0]):
+        assert np.array_equal(out["vertex_normal"][c].view(np.uint32), vn.view(np.uint32))
+
+
+def test_forward_structure_single_view():
+    s = small_scene(num_faces=5120, views=1, size=128, pitch=0.0)
+    out = oracle_scene(s).forward()
+    face, bary, render = out["face"][0], out["bary"][0], out["render"][0]
+    cov = face >= 0
+    # sphere of radius ~1000 mm at 3 m, 40 deg fov -> projected radius ~ 0.35 of the half-width
+    f = 64 / np.tan(np.radians(20))
+    r_px = f * 1000 / np.sqrt(3000 ** 2 - 1000 ** 2)
+    assert abs(cov.mean() - np.pi * r_px ** 2 / 128 ** 2) < 0.03
+    assert np.all(render[~cov] == [0.0, 1.0, 0.0])            # green background
+    assert np.all(bary[~cov] == 0)
+    a, b = bary[cov][:, 0], bary[cov][:, 1]
+    c = (f32(1) - a) - b
+    assert a.min() >= -0.001 and b.min() >= -0.001 and c.min() >= -0.001 and max(a.max(), b.max(), c.max()) <= 1.001
+    d = out["depth"][0][cov]                                   # camera z in units of 0.1 um
+    assert d.min() > 18000000 and d.max() < 32000000           # front cap of a 1 m sphere 3 m away
+
+
+def test_duplicate_face_is_a_tie_resolved_to_min_id():
+    s = small_scene(num_faces=320, views=1, size=48, pitch=0.0)
+    faces = np.concatenate([s["faces"], s["faces"][:40]])     # faces F..F+39 duplicate 0..39
+    uvs = np.concatenate([s["uvs"], s["uvs"][:40]])
+    from oracle.oracle import OracleScene
+    o = OracleScene(faces, uvs, s["vertex_pos"][0], s["vertex_color"][0], s["texture"][0], s["sh_coeff"][0],
+                    s["extrinsics"][0], s["intrinsics"][0], 48, 48)
+    out = o.forward()
+    F0 = s["faces"].shape[0]
+    dup = np.isin(out["face"], np.arange(40))
+    assert dup.any()
+    assert np.all(out["ties"][dup] >= 2)
+    tf = out["tie_faces"][dup]
+    assert np.all(np.any(tf == out["face"][dup][:, None] + F0, axis=1))
+
+
+def test_modes_forward_semantics():
+    s = small_scene(views=1, size=48)
+    base = oracle_scene(s).forward()
+    cov = base["face"][0] >= 0
+    fg = oracle_scene(s, albedo="foregroundMask", shading="shaded").forward()      # forced shadeless
+    assert np.all(fg["render"][0][cov] == 1.0)
+    nm = oracle_scene(s, albedo="normal", shading="shaded").forward()              # never shaded
+    assert nm["render"][0][cov].min() >= 0.0 and nm["render"][0][cov].max() <= 1.0
+    lt = oracle_scene(s, albedo="lighting", shading="shadeless").forward()         # always shaded
+    assert not np.allclose(lt["render"][0][cov], 1.0)
+    for o in (fg, nm, lt):
+        assert np.array_equal(o["face"], base["face"])
+
+
+def test_zero_gradient_modes():
+    s = small_scene(views=1, size=32)
+    for mode in ("normal", "lighting"):
+        o = oracle_scene(s, albedo=mode)
+        out = o.forward()
+        g = o.backward(out["face"], out["bary"], out["vertex_normal"], s["grad_render"][0], s["target_image"][0],
+                       s["grad_target"][0])
+        assert all(np.all(v == 0) for v in g.values())
+
+
+# ---------------------------------------------------------------------------- finite differences (FP64)
+
+def _fd_setup(albedo, shading="shaded", const_albedo=False, seed=3):
+    s = small_scene(num_faces=180, views=2, size=40, albedo=albedo, shading=shading, tex=8, seed=seed)
+    if const_albedo:
+        s["vertex_color"][:] = 0.7
+    o = oracle_scene(s)
+    out = o.forward()
+    _, flags = o.render_fp64(out["face"])
+    G = s["grad_render"][0].astype(np.float64)
+    G[flags != 0] = 0.0          # no flipped or grazing pixels: the reference gradient skips/ignores them
+    G = G.astype(np.float32)
+    g = o.backward(out["face"], out["bary"], out["vertex_normal"], G, s["target_image"][0], s["grad_target"][0])
+    return s, o, out, G.astype(np.float64), g
+
+
+def test_fd_vertex_position_grad_constant_albedo():
+    s, o, out, G, g = _fd_setup("vertexColor", const_albedo=True)
+    v0 = s["vertex_pos"][0].astype(np.float64)
+    h = 1e-4
+    fd = np.zeros_like(v0)
+    for i in range(v0.shape[0]):
+        for a in range(3):
+            vp, vm = v0.copy(), v0.copy()
+            vp[i, a] += h
+            vm[i, a] -= h
+            rp, _ = o.render_fp64(out["face"], vp)
+            rm, _ = o.render_fp64(out["face"], vm)
+            fd[i, a] = ((rp - rm) * G).sum() / (2 * h)
+    assert np.linalg.norm(fd) > 1e-3
+    assert rel_norm(g["vertex_pos_grad"], fd) < 1e-4
+
+
+def test_fd_vertex_color_and_sh_grads():
+    s, o, out, G, g = _fd_setup("vertexColor")
+    r0, _ = o.render_fp64(out["face"])
+    # linear in colours and SH coefficients: one-sided differences with a large step are exact up to rounding
+    col = s["vertex_color"][0].astype(np.float64)
+    fd = np.zeros_like(col)
+    for i in range(col.shape[0]):
+        for a in range(3):
+            c2 = col.copy()
+            c2[i, a] += 0.25
+            r1, _ = o.with_(colors=c2).render_fp64(out["face"])
+            fd[i, a] = ((r1 - r0) * G).sum() / 0.25
+    assert rel_norm(g["vertex_color_grad"], fd) < 1e-5
+    sh = s["sh_coeff"][0].astype(np.float64)
+    fdsh = np.zeros_like(sh)
+    for c in range(sh.shape[0]):
+        for k in range(27):
+            s2 = sh.copy()
+            s2[c, k] += 0.25
+            r1, _ = o.with_(sh=s2).render_fp64(out["face"])
+            fdsh[c, k] = ((r1 - r0) * G).sum() / 0.25
+    assert rel_norm(g["sh_coeff_grad"], fdsh) < 1e-5
+
+
+def test_fd_texture_grad():
+    s, o, out, G, g = _fd_setup("textured")
+    r0, _ = o.render_fp64(out["face"])
+    tex = s["texture"][0].astype(np.float64)
+    fd = np.zeros_like(tex)
+    for y in range(tex.shape[0]):
+        for x in range(tex.shape[1]):
+            for a in range(3):
+                t2 = tex.copy()
+                t2[y, x, a] += 0.25
+                r1, _ = o.with_(texture=t2).render_fp64(out["face"])
+                fd[y, x, a] = ((r1 - r0) * G).sum() / 0.25
+    assert np.linalg.norm(fd) > 0
+    assert rel_norm(g["texture_grad"], fd) < 1e-5
+
+
+def test_bary_jacobian_closed_form_matches_restatement():
+    """The kernels use d(bary)/d(v_j) = -b_j [g1, g2, -(g1+g2)] with
+    g1 = (e2 x d)/(N.d), g2 = (d x e1)/(N.d); the oracle restates the
+    reference's dJBCDVerpos term by term.  Their vertex-position gradients
+    must agree to FP64 rounding on a shaded scene with constant albedo
+    (where both equal the finite differences above)."""
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        v = rng.normal(0, 100, (3, 3)) + np.array([0, 0, 3000.0])
+        o = np.zeros(3)
+        d = v.mean(0) + rng.normal(0, 5, 3)
+        d /= np.linalg.norm(d)
+        e1, e2 = v[1] - v[0], v[2] - v[0]
+        N = np.cross(e1, e2)
+        g1, g2 = np.cross(e2, d) / N.dot(d), np.cross(d, e1) / N.dot(d)
+
+        def bary(vv):
+            n = np.cross(vv[1] - vv[0], vv[2] - vv[0])
+            t = (vv[0] - o).dot(n) / d.dot(n)
+            P = o + t * d
+            den = n.dot(n)
+            a = n.dot(np.cross(vv[2] - vv[1], P - vv[1])) / den
+            b = n.dot(np.cross(vv[0] - vv[2], P - vv[2])) / den
+            return np.array([a, b, 1 - a - b])
+        b0 = bary(v)
+        for j in range(3):
+            for k in range(3):
+                vp, vm = v.copy(), v.copy()
+                vp[j, k] += 1e-4
+                vm[j, k] -= 1e-4
+                fd = (bary(vp) - bary(vm)) / 2e-4
+                closed = -b0[j] * np.array([-(g1 + g2)[k], g1[k], g2[k]])
+                assert np.allclose(fd, closed, rtol=1e-5, atol=1e-9)
