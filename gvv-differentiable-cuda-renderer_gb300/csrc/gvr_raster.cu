@@ -4,17 +4,20 @@
 //
 // The reference tests every pixel of every face's box with its FP32
 // world-space ray/triangle test and keeps the smallest quantised depth.
-// Here each thread owns one pixel and the warps walk the tile's face
-// entries (staged in shared memory) twice with cheap screen-space bounds:
+// Here each thread owns one pixel; the tile's face entries are staged in
+// shared memory, sorted front to back by a lower bound of their depth, and
+// each warp walks them once with cheap screen-space bounds:
 //
-//   A  faces that certainly cover the pixel lower its depth bound zup
-//      (the face's exact quantised depth is <= zup);
-//   B  faces that may still win the pixel (not certainly outside, and not
-//      certainly deeper than zup + 2 units) become its candidates;
+//   - a face that certainly covers the pixel lowers the pixel's depth bound
+//     zup (the face's exact quantised depth is <= zup);
+//   - a face that may still win (not certainly outside, not certainly
+//     deeper than zup) is kept as a candidate (face, lower depth bound);
+//   - once the next entry's depth lower bound exceeds zup at every pixel of
+//     the warp, no later entry can matter and the warp stops.
 //
-// then the resolve runs the reference's exact test on the candidates only
-// and keeps the packed depth|face minimum.  Every skipped face provably has
-// a larger quantised depth than a face the exact test accepts, so the face
+// The resolve runs the reference's exact test on the surviving candidates
+// only and keeps the packed depth|face minimum.  Every skipped face provably
+// has a larger quantised depth than a face the exact test accepts, so face
 // ids and barycentrics equal those of testing every face (ties between
 // equal depths go to the smallest face id; the reference resolves them by a
 // write race).
@@ -79,15 +82,7 @@ __device__ __forceinline__ float entry_depth(const Entry &E, float l0, float l1,
     return 10000.0f * __fdividef(S, T);
 }
 
-// Pass A test: depth upper bound if the face certainly covers the pixel, else +inf.
-__device__ __forceinline__ float certain_zup(const Entry &E, float px, float py) {
-    float l0, l1, l2;
-    entry_lambda(E, px, py, l0, l1, l2);
-    if (l0 >= E.mIn && l1 >= E.mIn && l2 >= E.mIn) return entry_depth(E, l0, l1, l2) * (1.0f + E.dRel) + 2.0f;
-    return __int_as_float(0x7f800000);
-}
-
-// Pass B test: may the face win the pixel against the certain bound zup?
+// May the face win the pixel against the certain depth bound zup?
 __device__ __forceinline__ bool may_win(const Entry &E, float px, float py, float zup) {
     if (!(E.flags & kScreenValid)) return true;
     float l0, l1, l2;
@@ -132,7 +127,7 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     const int s0 = ws.tileStart[tIdx], nTile = ws.tileStart[tIdx + 1] - s0;
     const int nAll = nTile + ws.bigCount[bc];
 
-    // stage the entries whose box meets the tile (compacted; order does not matter)
+    // stage the entries whose box meets the tile (compacted in any order)
     if (tid == 0) sCount = 0;
     __syncthreads();
     for (int e = tid; e < nAll; e += kTilePix) {
@@ -147,41 +142,92 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     const bool overflow = nE > kCachedEntries;  // block-uniform: then walk the global list instead
     const int rowLo = tileY0 + 2 * (tid >> 5), rowHi = rowLo + 1;  // the two rows of this warp
 
-    auto entry_at = [&](int e, Entry &E) -> bool {
+    // front-to-back order by the entries' depth lower bound (rank sort; ties by slot)
+    __shared__ short sOrder[kCachedEntries];
+    if (!overflow) {
+        for (int e = tid; e < nE; e += kTilePix) {
+            const float k = sE[e].zLowSafe;
+            int rank = 0;
+            for (int j = 0; j < nE; ++j) {
+                const float kj = sE[j].zLowSafe;
+                rank += (kj < k) || (kj == k && j < e);
+            }
+            sOrder[rank] = (short)e;
+        }
+    }
+    __syncthreads();
+
+    auto entry_at = [&](int i, Entry &E) -> bool {
         if (!overflow) {
-            E = sE[e];
+            E = sE[sOrder[i]];
             return true;
         }
-        const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
+        const int f = i < nTile ? ws.bins[s0 + i] : bigList[i - nTile];
         E = make_entry(VF[f], f, tileX0, tileY0);
         return E.bx0 <= E.bx1 && E.by0 <= E.by1;
     };
     const int nWalk = overflow ? nAll : nE;
+    const float kInf = __int_as_float(0x7f800000);
 
-    // pass A: certain depth bound
-    float zup = __int_as_float(0x7f800000);
-    for (int e = 0; e < nWalk; ++e) {
-        Entry E;
-        if (!entry_at(e, E)) continue;
-        if (!(E.flags & kCertain) || E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
-        if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
-        zup = fminf(zup, certain_zup(E, px, py));
+    // One pass front to back: `zup` is the smallest certain depth bound so
+    // far; candidates (face, lower depth bound) are kept while their bound
+    // does not exceed it.  A bound only decreases, so a face dropped early
+    // could never win; the survivors are filtered again by the final bound.
+    float zup = kInf;
+    int nCand = 0;
+    bool spill = false;
+    int cf[kMaxCand];
+    float cz[kMaxCand];
+#pragma unroll
+    for (int j = 0; j < kMaxCand; ++j) {
+        cf[j] = -1;
+        cz[j] = kInf;
     }
-
-    // pass B: candidates (the last kMaxCand are kept; more means the slow path)
-    int cnt = 0, c0 = -1, c1 = -1, c2 = -1, c3 = -1;
-    for (int e = 0; e < nWalk; ++e) {
+    for (int i = 0; i < nWalk; ++i) {
         Entry E;
-        if (!entry_at(e, E)) continue;
+        if (!entry_at(i, E)) continue;
+        // every later entry lies behind every pixel of this warp: stop (sorted order only)
+        if (!overflow && E.zLowSafe > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
         if (E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
         if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
-        if (may_win(E, px, py, zup)) {
-            c3 = c2;
-            c2 = c1;
-            c1 = c0;
-            c0 = E.f;
-            ++cnt;
+        float zlow = -kInf;
+        if (E.flags & kScreenValid) {
+            float l0, l1, l2;
+            entry_lambda(E, px, py, l0, l1, l2);
+            if (l0 < -E.mOut || l1 < -E.mOut || l2 < -E.mOut) continue;  // certainly outside
+            const float zq = entry_depth(E, l0, l1, l2);
+            if ((E.flags & kCertain) && l0 >= E.mIn && l1 >= E.mIn && l2 >= E.mIn)
+                zup = fminf(zup, zq * (1.0f + E.dRel) + 2.0f);
+            zlow = E.zLowSafe;
+            if (E.dRel < 0.25f) zlow = fmaxf(zlow, zq * (1.0f - E.dRel) - 2.0f);
+            if (zlow > zup) continue;  // certainly behind a covering face
         }
+        if (nCand == kMaxCand) {  // make room: drop candidates now known to lose
+            int m = 0;
+#pragma unroll
+            for (int j = 0; j < kMaxCand; ++j) {
+                const bool keep = !(cz[j] > zup);
+#pragma unroll
+                for (int t = 0; t < kMaxCand; ++t)
+                    if (keep && t == m) {
+                        cf[t] = cf[j];
+                        cz[t] = cz[j];
+                    }
+                m += keep;
+            }
+            nCand = m;
+        }
+        if (nCand == kMaxCand) {
+            spill = true;
+            continue;
+        }
+#pragma unroll
+        for (int t = 0; t < kMaxCand; ++t)
+            if (t == nCand) {
+                cf[t] = E.f;
+                cz[t] = zlow;
+            }
+        ++nCand;
     }
 
     if (u >= dims.W || v >= dims.H) return;
@@ -195,19 +241,18 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     x.d = pixel_ray(cam, u, v);
     unsigned long long best = kEmptyKey;
     V3 abc = v3(0.0f, 0.0f, 0.0f);
-    if (cnt <= kMaxCand) {
-        const int cs[kMaxCand] = {c0, c1, c2, c3};
+    if (!spill) {
 #pragma unroll
-        for (int i = 0; i < kMaxCand; ++i) {
-            if (i >= cnt) break;
+        for (int j = 0; j < kMaxCand; ++j) {
+            if (j >= nCand || cz[j] > zup) continue;
             V3 t;
-            const unsigned long long k = exact_key(x, cs[i], t);
+            const unsigned long long k = exact_key(x, cf[j], t);
             if (k < best) {
                 best = k;
                 abc = t;
             }
         }
-    } else {
+    } else {  // more candidates than registers: test every face that may win against the final bound
         for (int e = 0; e < nWalk; ++e) {
             Entry E;
             if (!entry_at(e, E)) continue;
