@@ -406,34 +406,28 @@ __global__ void k_gather_b(const Topology topo, int B, const float *__restrict__
     for (int a = 0; a < 3; ++a) vpos_grad[3 * (size_t)i + a] += acc[a];
 }
 
-// One block per (batch, view): thread i sums tiles i, i+256, ... for all 27
-// coefficients in FP64, then a fixed-order tree finishes (deterministic).
+// One block per (batch, view, coefficient): thread i sums tiles i, i+256, ...
+// (FP32 with compensation), then a fixed-order FP64 tree finishes, so the
+// result is deterministic and FP64-accurate at FP32 cost.
 __global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
                                                      int tilesPerView, int shaded) {
-    __shared__ double red[8][27];
-    const int bc = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double s[27];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) s[k] = 0.0;
+    __shared__ double red[256];
+    const int bc = blockIdx.x / 27, k = blockIdx.x % 27;
+    float s = 0.0f, comp = 0.0f;
     if (shaded)
         for (int t = threadIdx.x; t < tilesPerView; t += 256) {
-            const float *p = partial + ((size_t)bc * tilesPerView + t) * 27;
-#pragma unroll
-            for (int k = 0; k < 27; ++k) s[k] += (double)p[k];
+            float hi, lo;
+            two_sum(s, partial[((size_t)bc * tilesPerView + t) * 27 + k], hi, lo);
+            s = hi;
+            comp += lo;
         }
-#pragma unroll
-    for (int k = 0; k < 27; ++k) {
-        double x = s[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) red[warp][k] = x;
-    }
+    red[threadIdx.x] = (double)s + (double)comp;
     __syncthreads();
-    if (threadIdx.x < 27) {
-        double tot = 0.0;
-        for (int w = 0; w < 8; ++w) tot += red[w][threadIdx.x];
-        sh_grad[(size_t)bc * 27 + threadIdx.x] = (float)tot;
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
     }
+    if (threadIdx.x == 0) sh_grad[(size_t)bc * 27 + k] = (float)red[0];
 }
 
 // ---------------------------------------------------------------------------- host launch
@@ -493,7 +487,7 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
                    k_gather_b<<<blocks((size_t)B * N, 256), 256, 0, st>>>(topo, B, a.vertex_pos, ws.gN, a.vertex_pos_grad));
         if ((err = cudaGetLastError())) return err;
     }
-    GVR_LAUNCH(st, "k_sh_finalize", k_sh_finalize<<<B * C, 256, 0, st>>>(ws.shPartial, a.sh_coeff_grad, T, shaded));
+    GVR_LAUNCH(st, "k_sh_finalize", k_sh_finalize<<<B * C * 27, 256, 0, st>>>(ws.shPartial, a.sh_coeff_grad, T, shaded));
     return cudaGetLastError();
 }
 

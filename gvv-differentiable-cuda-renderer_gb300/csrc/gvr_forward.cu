@@ -251,7 +251,9 @@ __global__ void k_bin_count(const Topology topo, const float *__restrict__ verts
     ViewFace vf;
     vf.hdr = make_int4(box.x | (box.z << 16), box.y | (box.w << 16), flags, __float_as_int(dRel));
     vf.z = make_float4(p0.z, p1.z, p2.z, mIn);
-    vf.s0 = make_float4(p0.x, p0.y, mOut, zmn * (10000.0f / 1.0025f) - 2.0f);
+    // any accepted depth is >= zmin / 1.002 when all z > 0 and z_max / z_min is moderate
+    // (barycentrics >= -0.001 summing to 1); otherwise no bound
+    vf.s0 = make_float4(p0.x, p0.y, mOut, valid ? zmn * (10000.0f / 1.0025f) - 2.0f : -__int_as_float(0x7f800000));
     vf.s1 = s1;
     ws.vface[i] = vf;
     if (box.x > box.z || box.y > box.w) return;

@@ -82,6 +82,20 @@ __device__ __forceinline__ float entry_depth(const Entry &E, float l0, float l1,
     return 10000.0f * __fdividef(S, T);
 }
 
+// False when no pixel centre of the entry's clipped box can pass the
+// "not certainly outside" test: each screen barycentric is affine, so its
+// maximum over the box is at the corner picked by the signs of its slopes.
+__device__ __forceinline__ bool may_cover_rect(const Entry &E) {
+    if (!(E.flags & kScreenValid)) return true;
+    const float xl = E.bx0 + 0.5f, xh = E.bx1 + 0.5f, yl = E.by0 + 0.5f, yh = E.by1 + 0.5f;
+    const float a0 = -(E.a1 + E.a2), b0 = -(E.b1 + E.b2);
+    float l0, l1, l2, s, t;
+    entry_lambda(E, a0 >= 0.0f ? xh : xl, b0 >= 0.0f ? yh : yl, l0, s, t);
+    entry_lambda(E, E.a1 >= 0.0f ? xh : xl, E.b1 >= 0.0f ? yh : yl, s, l1, t);
+    entry_lambda(E, E.a2 >= 0.0f ? xh : xl, E.b2 >= 0.0f ? yh : yl, s, t, l2);
+    return !(l0 < -E.mOut || l1 < -E.mOut || l2 < -E.mOut);
+}
+
 // May the face win the pixel against the certain depth bound zup?
 __device__ __forceinline__ bool may_win(const Entry &E, float px, float py, float zup) {
     if (!(E.flags & kScreenValid)) return true;
@@ -127,15 +141,31 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     const int s0 = ws.tileStart[tIdx], nTile = ws.tileStart[tIdx + 1] - s0;
     const int nAll = nTile + ws.bigCount[bc];
 
-    // stage the entries whose box meets the tile (compacted in any order)
+    // stage the entries whose triangle may cover a pixel of the tile (compacted in any order)
+    __shared__ float sKey[kCachedEntries];
     if (tid == 0) sCount = 0;
     __syncthreads();
-    for (int e = tid; e < nAll; e += kTilePix) {
-        const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
-        const Entry E = make_entry(VF[f], f, tileX0, tileY0);
-        if (E.bx0 > E.bx1 || E.by0 > E.by1) continue;
-        const int slot = atomicAdd(&sCount, 1);
-        if (slot < kCachedEntries) sE[slot] = E;
+    const int lane = tid & 31;
+    for (int e0 = 0; e0 < nAll; e0 += kTilePix) {
+        const int e = e0 + tid;
+        bool keep = false;
+        Entry E;
+        if (e < nAll) {
+            const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
+            E = make_entry(VF[f], f, tileX0, tileY0);
+            keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        int base = 0;
+        if (lane == 0 && m) base = atomicAdd(&sCount, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (keep) {
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            if (slot < kCachedEntries) {
+                sE[slot] = E;
+                sKey[slot] = E.zLowSafe;
+            }
+        }
     }
     __syncthreads();
     const int nE = sCount;
@@ -146,10 +176,10 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     __shared__ short sOrder[kCachedEntries];
     if (!overflow) {
         for (int e = tid; e < nE; e += kTilePix) {
-            const float k = sE[e].zLowSafe;
+            const float k = sKey[e];
             int rank = 0;
             for (int j = 0; j < nE; ++j) {
-                const float kj = sE[j].zLowSafe;
+                const float kj = sKey[j];
                 rank += (kj < k) || (kj == k && j < e);
             }
             sOrder[rank] = (short)e;
@@ -190,6 +220,7 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
         if (!overflow && E.zLowSafe > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
         if (E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
         if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
+        if (E.zLowSafe > zup) continue;  // behind this pixel's covering face (and so is every later entry)
         float zlow = -kInf;
         if (E.flags & kScreenValid) {
             float l0, l1, l2;
