@@ -144,6 +144,20 @@ def test_zero_gradient_modes():
         assert all(np.all(v == 0) for v in g.values())
 
 
+def test_refcore_parameter_struct_layout():
+    """The harness that runs the reference kernels restates their by-value
+    parameter structs; their offsets must equal those compiled from the
+    reference headers (recorded in oracle/_ref/layout.json by the build)."""
+    import json
+    import os
+    import shutil
+    from oracle import refcore
+    path = os.path.join(refcore.REF_DIR, "layout.json")
+    if not os.path.exists(path) or not shutil.which("nvcc"):
+        pytest.skip("reference layout not recorded")
+    assert refcore.harness_layout() == json.load(open(path))
+
+
 # ---------------------------------------------------------------------------- finite differences (FP64)
 
 def _fd_setup(albedo, shading="shaded", const_albedo=False, seed=3):
