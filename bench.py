@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--impl", choices=["gvr", "reference"], default="gvr")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bound of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
+    ap.add_argument("--views", type=int, default=8, help="views of the workload (profiling runs use fewer)")
     return ap.parse_args()
 
 
@@ -227,7 +229,7 @@ def run_gvr(args):
     native_build.build()
     L = _lib.load()
 
-    s = scenes.multiview_textured(seed=rank)
+    s = scenes.multiview_textured(seed=rank, num_views=args.views)
     B, C, H, W = 1, s["num_views"], s["height"], s["width"]
     N, F = s["num_vertices"], s["faces"].shape[0]
     Ht, Wt = s["texture"].shape[1], s["texture"].shape[2]
@@ -325,18 +327,20 @@ def run_gvr(args):
         for k, v in hres.items():
             v.copy_(out[k], non_blocking=True)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    barrier(world)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world)
-    barrier(world)
+    e2e_ms = float("nan")
+    if not args.no_e2e:
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world)
+        barrier(world)
 
     if rank != 0:
         return

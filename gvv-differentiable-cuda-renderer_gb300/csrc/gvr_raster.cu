@@ -28,7 +28,8 @@
 namespace gvr {
 namespace {
 
-constexpr int kCachedEntries = 512;  // compacted face entries of a tile kept in shared memory
+constexpr int kCachedEntries = 320;  // compacted face entries of a tile kept in shared memory
+constexpr int kBuckets = 64;         // depth buckets of the front-to-back order
 constexpr int kMaxCand = 4;          // candidates a pixel keeps in registers
 
 // Face entry with its skip-test constants and its box clipped to the tile (80 bytes).
@@ -114,11 +115,14 @@ struct ExactCtx {
     V3 d;
 };
 
-// The reference's exact test of face f at this pixel; key = kEmptyKey if rejected.
-__device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f, V3 &abc) {
+// The reference's exact test of face f at this pixel; key = kEmptyKey if
+// rejected.  With needDepth = false (a single candidate) the key of an
+// accepted face is just its id: only acceptance matters then.
+__device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f, V3 &abc, bool needDepth) {
     const FaceSetup fs = load_face(&x.geo[f]);
     abc = barycentric(fs, x.origS, xdot(x.origS, fs.n), x.d);
     if (!inside(abc)) return kEmptyKey;
+    if (!needDepth) return (unsigned long long)(unsigned)f;
     const float4 z = x.vface[f].z;
     return depth_key(depth_quantised(abc, z.x, z.y, z.z), f);
 }
@@ -172,17 +176,53 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     const bool overflow = nE > kCachedEntries;  // block-uniform: then walk the global list instead
     const int rowLo = tileY0 + 2 * (tid >> 5), rowHi = rowLo + 1;  // the two rows of this warp
 
-    // front-to-back order by the entries' depth lower bound (rank sort; ties by slot)
+    // Front-to-back order: counting sort into kBuckets depth buckets spanning
+    // the tile's finite depth lower bounds (faces without a bound go first).
+    // sBucketLo[i] is a lower bound of the depth bound of entry i and of
+    // every entry after it, which is all the early exit needs.
     __shared__ short sOrder[kCachedEntries];
+    __shared__ float sBucketLo[kCachedEntries];
+    __shared__ int sHist[kBuckets + 1];
+    __shared__ unsigned sKeyLo, sKeyHi;
     if (!overflow) {
+        if (tid == 0) {
+            sKeyLo = 0x7f800000u;
+            sKeyHi = 0u;
+        }
+        if (tid <= kBuckets) sHist[tid] = 0;
+        __syncthreads();
         for (int e = tid; e < nE; e += kTilePix) {
             const float k = sKey[e];
-            int rank = 0;
-            for (int j = 0; j < nE; ++j) {
-                const float kj = sKey[j];
-                rank += (kj < k) || (kj == k && j < e);
+            if (k >= 0.0f && k < __int_as_float(0x7f800000)) {  // finite, non-negative: order like unsigned ints
+                atomicMin(&sKeyLo, __float_as_uint(k));
+                atomicMax(&sKeyHi, __float_as_uint(k));
             }
-            sOrder[rank] = (short)e;
+        }
+        __syncthreads();
+        const float lo = __uint_as_float(sKeyLo), hi = __uint_as_float(sKeyHi);
+        const float scale = hi > lo ? (float)kBuckets / (hi - lo) : 0.0f;
+        auto bucket_of = [&](float k) -> int {  // 0: no usable bound; 1..kBuckets by depth
+            if (!(k >= lo)) return 0;
+            return 1 + min(kBuckets - 1, (int)((k - lo) * scale));
+        };
+        for (int e = tid; e < nE; e += kTilePix) atomicAdd(&sHist[bucket_of(sKey[e])], 1);
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0;
+            for (int q = 0; q <= kBuckets; ++q) {
+                const int c = sHist[q];
+                sHist[q] = run;
+                run += c;
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < nE; e += kTilePix) {
+            const int q = bucket_of(sKey[e]);
+            const int pos = atomicAdd(&sHist[q], 1);
+            sOrder[pos] = (short)e;
+            // the bucket's lower edge, pulled down by 0.1% of its offset so rounding
+            // in bucket_of can never leave a member below it
+            sBucketLo[pos] = q == 0 ? -__int_as_float(0x7f800000) : q == 1 ? lo : lo + (float)(q - 1) * (0.999f / scale);
         }
     }
     __syncthreads();
@@ -217,7 +257,7 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
         Entry E;
         if (!entry_at(i, E)) continue;
         // every later entry lies behind every pixel of this warp: stop (sorted order only)
-        if (!overflow && E.zLowSafe > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
+        if (!overflow && sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
         if (E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
         if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
         if (E.zLowSafe > zup) continue;  // behind this pixel's covering face (and so is every later entry)
@@ -273,11 +313,14 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     unsigned long long best = kEmptyKey;
     V3 abc = v3(0.0f, 0.0f, 0.0f);
     if (!spill) {
+        int nLive = 0;
+#pragma unroll
+        for (int j = 0; j < kMaxCand; ++j) nLive += (j < nCand && !(cz[j] > zup));
 #pragma unroll
         for (int j = 0; j < kMaxCand; ++j) {
             if (j >= nCand || cz[j] > zup) continue;
             V3 t;
-            const unsigned long long k = exact_key(x, cf[j], t);
+            const unsigned long long k = exact_key(x, cf[j], t, nLive > 1);
             if (k < best) {
                 best = k;
                 abc = t;
@@ -290,7 +333,7 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
             if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
             if (!may_win(E, px, py, zup)) continue;
             V3 t;
-            const unsigned long long k = exact_key(x, E.f, t);
+            const unsigned long long k = exact_key(x, E.f, t, true);
             if (k < best) {
                 best = k;
                 abc = t;
