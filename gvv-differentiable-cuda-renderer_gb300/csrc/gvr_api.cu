@@ -2,6 +2,7 @@
 // workspace layout and dispatch.  Errors are returned, never fatal.
 #include <climits>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -356,3 +357,49 @@ int gvr_debug_rays(GvrHandle *h, int32_t batch, const float *extr, const float *
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------- backward without allocation
+//
+// Scratch for gvr_backward_noalloc: a fixed device array that every GPU
+// loading this library holds until the process exits.  In host code the
+// symbol is only a stand-in, so its device address is looked up once per
+// device (with that device current) and cached.
+
+namespace {
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[GVR_NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+std::vector<void *> g_noalloc_addr;  // per device ordinal
+
+}  // namespace
+
+extern "C" int gvr_backward_noalloc(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
+    if (!h || !a) return fail(GVR_ERR_INVALID_ARGUMENT, "handle/args is NULL");
+    const size_t need = gvr_backward_workspace_size(h, a->batch, a->texture_height, a->texture_width);
+    if (need == 0) return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1");
+    if (need > GVR_NOALLOC_SCRATCH_BYTES)
+        return fail(GVR_ERR_WORKSPACE, "gvr_backward_noalloc: this call needs " + std::to_string(need) +
+                                           " bytes of scratch but the library's fixed scratch array holds " +
+                                           std::to_string((size_t)GVR_NOALLOC_SCRATCH_BYTES) +
+                                           "; use gvr_backward with a workspace");
+    void *scratch = nullptr;
+    {
+        DeviceGuard g(h->device);
+        if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (h->device < 0) return fail(GVR_ERR_INVALID_ARGUMENT, "bad device");
+        if ((size_t)h->device >= g_noalloc_addr.size()) g_noalloc_addr.resize(h->device + 1, nullptr);
+        if (!g_noalloc_addr[h->device]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+            g_noalloc_addr[h->device] = p;
+        }
+        scratch = g_noalloc_addr[h->device];
+    }
+    GvrBackwardArgs args = *a;
+    args.workspace = scratch;
+    args.workspace_bytes = GVR_NOALLOC_SCRATCH_BYTES;
+    return gvr_backward(h, &args, stream);
+}

@@ -51,7 +51,9 @@ class GvrKernelTime(ctypes.Structure):
 # Every symbol include/gvr.h declares.
 EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forward_workspace_size",
            "gvr_backward_workspace_size", "gvr_last_error", "gvr_abi_version", "gvr_debug_rays",
-           "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count")
+           "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc")
+
+NOALLOC_SCRATCH_BYTES = 32 << 20  # GVR_NOALLOC_SCRATCH_BYTES
 
 _lib = None
 
@@ -90,6 +92,8 @@ def load(build_if_missing: bool = True):
     L.gvr_profile_read.restype = ctypes.c_int
     L.gvr_launch_count.argtypes = []
     L.gvr_launch_count.restype = ctypes.c_longlong
+    L.gvr_backward_noalloc.argtypes = [P, ctypes.POINTER(GvrBackwardArgs), P]
+    L.gvr_backward_noalloc.restype = ctypes.c_int
     _lib = L
     return L
 

@@ -157,6 +157,26 @@ int gvr_abi_version(void);
 int gvr_debug_rays(GvrHandle *handle, int32_t batch, const float *extrinsics, const float *intrinsics,
                    float *rays_out, void *stream);
 
+/* Backward pass that allocates nothing; it has no counterpart in the reference.
+ *
+ * For callers that must not allocate device memory while rendering: a host
+ * that hands this library a fixed memory budget up front (an engine or
+ * plugin host whose allocator owns the GPU), or code on a real-time path
+ * where a cudaMalloc would synchronise the device and stall the frame.
+ * The caller still passes every input and output buffer; the scratch the
+ * backward needs (per-face gradient accumulators, SH partial sums, camera and
+ * face records) lives in one device array of GVR_NOALLOC_SCRATCH_BYTES that
+ * the library reserves on each GPU it is loaded on, for the life of the
+ * process.  Calls needing more scratch than that (about 17 MiB for one batch
+ * element of 8 views at 1024x1024 and 70,000 faces) return
+ * GVR_ERR_WORKSPACE.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  Every call on a device shares the one array: calls that overlap
+ * on the GPU (other streams, other threads) race and corrupt each other's
+ * results; everything that must start at zero is cleared inside each call. */
+#define GVR_NOALLOC_SCRATCH_BYTES (32u << 20)
+int gvr_backward_noalloc(GvrHandle *handle, const GvrBackwardArgs *args, void *stream);
+
 /* Per-kernel timing, no reference counterpart.  While enabled, every kernel
  * the library launches is bracketed by a CUDA event pair on its stream;
  * gvr_profile_read waits for those events and reports, per kernel name, the
