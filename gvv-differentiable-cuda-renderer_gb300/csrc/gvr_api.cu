@@ -1,9 +1,13 @@
 // gvr_api.cu -- the C ABI (include/gvr.h): validation, topology upload,
 // workspace layout and dispatch.  Errors are returned, never fatal.
+#include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "gvr_kernels.h"
@@ -66,26 +70,52 @@ struct Carver {
 struct FwdLayout {
     gvr::FwdScratch s;
     float4 *proj;
+    int *uvOwner;  // [Ht*Wt] face owning each texel (compute_normal_map only)
     size_t bytes;
 };
 
-FwdLayout fwd_layout(const GvrHandle *h, int B, void *base) {
-    const size_t BC = (size_t)B * h->attrs.num_cameras, T = (size_t)h->tilesX * h->tilesY;
-    Carver c(base);
-    FwdLayout L{};
+// Tile shape (w x h = 256 pixels, w in {8, 16, 32}) and big-face threshold
+// of the forward binning.  Every choice gives the same pixels.
+struct TileCfg {
+    int w = gvr::kTile, h = gvr::kTile, big = gvr::kBigTiles;
+    int tilesX(const GvrHandle *hd) const { return (hd->attrs.render_resolution_u + w - 1) / w; }
+    int tilesY(const GvrHandle *hd) const { return (hd->attrs.render_resolution_v + h - 1) / h; }
+    bool valid() const { return (w == 8 || w == 16 || w == 32) && w * h == gvr::kTilePix && big >= 1 && big <= 64; }
+};
+
+// Buffers of one forward call except the per-call zeroed counters.
+void fwd_carve_main(const GvrHandle *h, int B, int Ht, int Wt, const TileCfg &tc, Carver &c, FwdLayout &L) {
+    const size_t BC = (size_t)B * h->attrs.num_cameras, T = (size_t)tc.tilesX(h) * tc.tilesY(h);
     L.s.cams = c.take<gvr::Camera>(BC);
     L.s.geo = c.take<gvr::FaceGeo>((size_t)B * h->F);
     L.s.fnormal = c.take<float4>((size_t)B * h->F);
     L.proj = c.take<float4>(BC * h->N);
+    if (h->attrs.compute_normal_map) {  // no binning: the depth and shading passes do not run
+        L.uvOwner = c.take<int>((size_t)(Ht > 0 ? Ht : 1) * (Wt > 0 ? Wt : 1));
+        return;
+    }
     L.s.vface = c.take<gvr::ViewFace>(BC * h->F);
     L.s.tileStart = c.take<int>(BC * T + 1);
-    L.s.bins = c.take<int>((size_t)gvr::kBigTiles * BC * h->F);
+    L.s.bins = c.take<int>((size_t)tc.big * BC * h->F);
     L.s.bigList = c.take<int>(BC * h->F);
-    // per-call zeroed counters, contiguous
+}
+
+// The counters cleared before every call (tile counts and cursors, big-list counts).
+void fwd_carve_counters(const GvrHandle *h, int B, const TileCfg &tc, Carver &c, FwdLayout &L) {
+    if (h->attrs.compute_normal_map) return;
+    const size_t BC = (size_t)B * h->attrs.num_cameras, T = (size_t)tc.tilesX(h) * tc.tilesY(h);
     L.s.tileCount = c.take<int>(BC * T);
-    size_t z0 = c.off - BC * T * sizeof(int);
     L.s.tileCursor = c.take<int>(BC * T);
     L.s.bigCount = c.take<int>(BC);
+}
+
+FwdLayout fwd_layout(const GvrHandle *h, int B, int Ht, int Wt, void *base, const TileCfg &tc = TileCfg()) {
+    Carver c(base);
+    FwdLayout L{};
+    fwd_carve_main(h, B, Ht, Wt, tc, c, L);
+    c.take<char>(0);  // align
+    const size_t z0 = c.off;
+    fwd_carve_counters(h, B, tc, c, L);
     L.s.zeroBase = base ? c.base + z0 : nullptr;
     L.s.zeroBytes = c.off - z0;
     L.bytes = c.off + 256;
@@ -171,7 +201,6 @@ int gvr_create(const GvrTopology *topo, const GvrAttrs *attrs, GvrHandle **out) 
     // CudaRendererGrad.cpp:84-98
     if (attrs->image_filter_size <= 0) return fail(GVR_ERR_INVALID_ARGUMENT, "INVALID IMAGE FILTER SIZE");
     if (attrs->texture_filter_size <= 0) return fail(GVR_ERR_INVALID_ARGUMENT, "INVALID TEXTURE FILTER SIZE");
-    if (attrs->compute_normal_map) return fail(GVR_ERR_UNSUPPORTED, "compute_normal_map is not supported by this build");
     for (int i = 0; i < 3 * F; ++i)
         if (topo->faces[i] < 0 || topo->faces[i] >= N)
             return fail(GVR_ERR_INVALID_ARGUMENT, "face " + std::to_string(i / 3) + " references vertex " +
@@ -237,9 +266,9 @@ void gvr_destroy(GvrHandle *h) {
     delete h;
 }
 
-size_t gvr_forward_workspace_size(const GvrHandle *h, int32_t batch, int32_t, int32_t) {
+size_t gvr_forward_workspace_size(const GvrHandle *h, int32_t batch, int32_t texture_height, int32_t texture_width) {
     if (!h || batch < 1) return 0;
-    return fwd_layout(h, batch, nullptr).bytes;
+    return fwd_layout(h, batch, texture_height, texture_width, nullptr).bytes;
 }
 
 size_t gvr_backward_workspace_size(const GvrHandle *h, int32_t batch, int32_t, int32_t) {
@@ -247,25 +276,31 @@ size_t gvr_backward_workspace_size(const GvrHandle *h, int32_t batch, int32_t, i
     return bwd_layout(h, batch, nullptr).bytes;
 }
 
-static gvr::FrameDims dims_of(const GvrHandle *h, int B, int Ht, int Wt) {
+static gvr::FrameDims dims_of(const GvrHandle *h, int B, int Ht, int Wt, const TileCfg &tc = TileCfg()) {
     gvr::FrameDims d;
     d.B = B;
     d.C = h->attrs.num_cameras;
     d.W = h->attrs.render_resolution_u;
     d.H = h->attrs.render_resolution_v;
-    d.tilesX = h->tilesX;
-    d.tilesY = h->tilesY;
+    d.tilesX = tc.tilesX(h);
+    d.tilesY = tc.tilesY(h);
     d.Ht = Ht;
     d.Wt = Wt;
     d.albedo = h->attrs.albedo_mode;
     d.shading = h->attrs.shading_mode;
+    d.tileW = tc.w;
+    d.tileH = tc.h;
+    d.tileShift = tc.w == 8 ? 3 : tc.w == 16 ? 4 : 5;
+    d.bigTiles = tc.big;
     return d;
 }
 
-int gvr_forward(GvrHandle *h, const GvrForwardArgs *a, void *stream) {
+// Checks the forward arguments against the handle (shared by the per-call
+// and the batched forward).
+static int check_forward_args(const GvrHandle *h, const GvrForwardArgs *a) {
     if (!h || !a) return fail(GVR_ERR_INVALID_ARGUMENT, "handle/args is NULL");
-    const int B = a->batch;
-    if (!batch_fits(h, B)) return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1 and the call within int32 index range");
+    if (!batch_fits(h, a->batch))
+        return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1 and the call within int32 index range");
     const int mode = h->attrs.albedo_mode;
     const bool textured = mode == GVR_ALBEDO_TEXTURED;
     if (textured && (a->texture_height < 1 || a->texture_width < 1 || !a->texture))
@@ -278,29 +313,69 @@ int gvr_forward(GvrHandle *h, const GvrForwardArgs *a, void *stream) {
         return fail(GVR_ERR_INVALID_ARGUMENT, "barycentric, face, render and vertex_normal outputs are required");
     if (a->target_image_out && !a->target_image)
         return fail(GVR_ERR_INVALID_ARGUMENT, "target_image_out needs target_image");
-    DeviceGuard g(h->device);
-    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const FwdLayout need = fwd_layout(h, B, nullptr);
-    CallScratch scratch;
-    int rc = scratch.acquire(a->workspace, a->workspace_bytes, need.bytes, st);
-    if (rc != GVR_OK) return rc;
-    FwdLayout L = fwd_layout(h, B, scratch.ptr);
-    gvr::FrameDims dims = dims_of(h, B, textured ? a->texture_height : 1, textured ? a->texture_width : 1);
-    cudaError_t e = gvr::launch_forward(h->topo(), dims, L.s, a->vertex_pos, a->vertex_color, a->texture, a->sh_coeff,
-                                        a->extrinsics, a->intrinsics, a->barycentric, a->face, a->render,
-                                        a->vertex_normal, L.proj, st);
-    if (e != cudaSuccess) return cuda_fail(e, "forward launch");
+    if (h->attrs.compute_normal_map && (!a->normal_map || a->texture_height < 1 || a->texture_width < 1))
+        return fail(GVR_ERR_INVALID_ARGUMENT,
+                    "compute_normal_map needs the normal_map output and texture_height/width >= 1");
+    return GVR_OK;
+}
+
+// Texture size the forward uses (1x1 when neither textured nor normal-map).
+static void forward_texture_size(const GvrHandle *h, const GvrForwardArgs *a, int &Ht, int &Wt) {
+    const bool used = h->attrs.albedo_mode == GVR_ALBEDO_TEXTURED || h->attrs.compute_normal_map;
+    Ht = used ? a->texture_height : 1;
+    Wt = used ? a->texture_width : 1;
+}
+
+static gvr::FwdJob make_job(const GvrHandle *h, const GvrForwardArgs *a, const FwdLayout &L,
+                            const gvr::FrameDims &dims) {
+    gvr::FwdJob J;
+    J.topo = h->topo();
+    J.dims = dims;
+    J.ws = L.s;
+    J.io = gvr::RasterIO{a->vertex_pos, a->vertex_color, a->texture, a->sh_coeff, a->vertex_normal,
+                         a->barycentric, a->face, a->render};
+    J.extr = a->extrinsics;
+    J.intr = a->intrinsics;
+    J.proj = L.proj;
+    J.vnormal_out = a->vertex_normal;
+    return J;
+}
+
+// The work of gvr_forward after the frame: the target copy and the unused normal map.
+static int forward_epilogue(const GvrHandle *h, const GvrForwardArgs *a, cudaStream_t st) {
+    const int B = a->batch;
     const size_t img = (size_t)B * h->attrs.num_cameras * h->attrs.render_resolution_v * h->attrs.render_resolution_u * 3;
+    cudaError_t e;
     if (a->target_image_out && a->target_image_out != a->target_image) {
         e = cudaMemcpyAsync(a->target_image_out, a->target_image, img * sizeof(float), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return cuda_fail(e, "target_image_out copy");
     }
-    if (a->normal_map && a->texture_height > 0 && a->texture_width > 0) {
+    if (!h->attrs.compute_normal_map && a->normal_map && a->texture_height > 0 && a->texture_width > 0) {
         e = cudaMemsetAsync(a->normal_map, 0, (size_t)B * a->texture_height * a->texture_width * 3 * sizeof(float), st);
         if (e != cudaSuccess) return cuda_fail(e, "normal_map clear");
     }
     return GVR_OK;
+}
+
+int gvr_forward(GvrHandle *h, const GvrForwardArgs *a, void *stream) {
+    int rc = check_forward_args(h, a);
+    if (rc != GVR_OK) return rc;
+    const int B = a->batch;
+    DeviceGuard g(h->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int Ht, Wt;
+    forward_texture_size(h, a, Ht, Wt);
+    const FwdLayout need = fwd_layout(h, B, Ht, Wt, nullptr);
+    CallScratch scratch;
+    rc = scratch.acquire(a->workspace, a->workspace_bytes, need.bytes, st);
+    if (rc != GVR_OK) return rc;
+    const FwdLayout L = fwd_layout(h, B, Ht, Wt, scratch.ptr);
+    const gvr::FwdJob J = make_job(h, a, L, dims_of(h, B, Ht, Wt));
+    const cudaError_t e = h->attrs.compute_normal_map ? gvr::launch_forward_normal_map(J, L.uvOwner, a->normal_map, st)
+                                                      : gvr::launch_forward(J, st);
+    if (e != cudaSuccess) return cuda_fail(e, "forward launch");
+    return forward_epilogue(h, a, st);
 }
 
 int gvr_backward(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
@@ -403,3 +478,304 @@ extern "C" int gvr_backward_noalloc(GvrHandle *h, const GvrBackwardArgs *a, void
     args.workspace_bytes = GVR_NOALLOC_SCRATCH_BYTES;
     return gvr_backward(h, &args, stream);
 }
+
+// ---------------------------------------------------------------------------- batched forward plans
+
+struct GvrPlan {
+    int device = 0;
+    std::vector<GvrJob> jobs;
+    std::vector<TileCfg> tiles;
+    void *d_mem = nullptr;  // every job's scratch, the job tables and the zeroed counters
+    gvr::BatchLaunch launch{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Candidate bin/tile configurations of the autotuner: tile shapes of 256
+// pixels and the span (in tiles) above which a face goes to the view's
+// big-face list.
+const TileCfg kTuneCandidates[] = {{16, 16, 16}, {32, 8, 16}, {8, 32, 16}, {16, 16, 4}, {32, 8, 4}, {8, 32, 4}};
+
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, TileCfg> g_tune_cache;  // (floor(log2 F), W, H) -> fastest
+
+int log2_floor(int x) {
+    int k = 0;
+    while (k < 30 && (1 << (k + 1)) <= x) ++k;
+    return k;
+}
+
+// Times one forward of a job under every candidate configuration on a
+// private stream (CUDA events; one warm-up, median of three) and returns the
+// fastest.  The job's outputs are written, as by a normal forward.
+int autotune_job(const GvrHandle *h, const GvrForwardArgs *a, TileCfg &best) {
+    int Ht, Wt;
+    forward_texture_size(h, a, Ht, Wt);
+    size_t bytes = 0;
+    for (const TileCfg &c : kTuneCandidates) bytes = std::max(bytes, fwd_layout(h, a->batch, Ht, Wt, nullptr, c).bytes);
+    void *ws = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaMalloc(&ws, bytes);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    float bestMs = INFINITY;
+    best = TileCfg();
+    for (const TileCfg &c : kTuneCandidates) {
+        if (e != cudaSuccess) break;
+        const FwdLayout L = fwd_layout(h, a->batch, Ht, Wt, ws, c);
+        const gvr::FwdJob J = make_job(h, a, L, dims_of(h, a->batch, Ht, Wt, c));
+        float t[3];
+        e = gvr::launch_forward(J, st);
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
+            e = cudaEventRecord(ev[0], st);
+            if (e == cudaSuccess) e = gvr::launch_forward(J, st);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t[r], ev[0], ev[1]);
+        }
+        if (e != cudaSuccess) break;
+        std::sort(t, t + 3);
+        if (t[1] < bestMs) {
+            bestMs = t[1];
+            best = c;
+        }
+    }
+    if (st) cudaStreamSynchronize(st);
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    if (st) cudaStreamDestroy(st);
+    if (ws) cudaFree(ws);
+    return e == cudaSuccess ? GVR_OK : cuda_fail(e, "autotune");
+}
+
+int tile_config_for(const GvrHandle *h, const GvrForwardArgs *a, bool tune, TileCfg &out) {
+    out = TileCfg();
+    if (!tune) return GVR_OK;
+    const auto key = std::make_tuple(log2_floor(h->F), h->attrs.render_resolution_u, h->attrs.render_resolution_v);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            out = it->second;
+            return GVR_OK;
+        }
+    }
+    int rc = autotune_job(h, a, out);
+    if (rc != GVR_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = out;
+    return GVR_OK;
+}
+
+// Device tables of a plan, carved after every job's scratch.
+struct PlanTables {
+    gvr::FwdJob *jobs;
+    int *blockStart[gvr::kNumStages];
+    int *itemStart;
+    int *counter;
+};
+
+// Carves (or, with base == nullptr, measures) a plan's memory: every job's
+// scratch, the tables, then one zeroed region holding every job's counters
+// and the raster work counter.
+size_t plan_carve(const GvrPlan &p, void *base, std::vector<FwdLayout> &lay, PlanTables &t, size_t &z0,
+                  size_t &z1) {
+    const int J = (int)p.jobs.size();
+    Carver c(base);
+    lay.assign(J, FwdLayout{});
+    for (int j = 0; j < J; ++j) {
+        const GvrJob &job = p.jobs[j];
+        int Ht, Wt;
+        forward_texture_size(job.handle, &job.forward, Ht, Wt);
+        fwd_carve_main(job.handle, job.forward.batch, Ht, Wt, p.tiles[j], c, lay[j]);
+    }
+    t.jobs = c.take<gvr::FwdJob>(J);
+    for (int s = 0; s < gvr::kNumStages; ++s) t.blockStart[s] = c.take<int>(J + 1);
+    t.itemStart = c.take<int>(J + 1);
+    c.take<char>(0);
+    z0 = c.off;
+    for (int j = 0; j < J; ++j) fwd_carve_counters(p.jobs[j].handle, p.jobs[j].forward.batch, p.tiles[j], c, lay[j]);
+    t.counter = c.take<int>(1);
+    z1 = c.off;
+    return c.off + 256;
+}
+
+int plan_forward_body(GvrPlan *p, cudaStream_t st) {
+    cudaError_t e = gvr::launch_forward_batched(p->launch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "batched forward launch");
+    for (const GvrJob &job : p->jobs) {
+        const int rc = forward_epilogue(job.handle, &job.forward, st);
+        if (rc != GVR_OK) return rc;
+    }
+    return GVR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gvr_plan_create(const GvrJob *jobs, int32_t count, int32_t flags, GvrPlan **out_plan) {
+    if (!out_plan) return fail(GVR_ERR_INVALID_ARGUMENT, "out_plan is NULL");
+    *out_plan = nullptr;
+    if (!jobs || count < 1) return fail(GVR_ERR_INVALID_ARGUMENT, "a plan needs at least one job");
+    const int device = jobs[0].handle ? jobs[0].handle->device : -1;
+    for (int j = 0; j < count; ++j) {
+        if (jobs[j].handle && jobs[j].handle->attrs.compute_normal_map)
+            return fail(GVR_ERR_UNSUPPORTED, "job " + std::to_string(j) + ": normal-map handles run through gvr_forward");
+        const int rc = check_forward_args(jobs[j].handle, &jobs[j].forward);
+        if (rc != GVR_OK) return fail(rc, "job " + std::to_string(j) + ": " + g_error);
+        if (jobs[j].handle->device != device)
+            return fail(GVR_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + " is on another device");
+    }
+    DeviceGuard g(device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    GvrPlan *p = new GvrPlan();
+    p->device = device;
+    p->jobs.assign(jobs, jobs + count);
+    p->tiles.resize(count);
+    for (int j = 0; j < count; ++j) {
+        const GvrJob &job = jobs[j];
+        const bool forced = job.tile_width != 0 || job.big_tiles != 0;
+        int rc = GVR_OK;
+        if (forced) {
+            TileCfg c;
+            if (job.tile_width) {
+                c.w = job.tile_width;
+                c.h = job.tile_width > 0 ? gvr::kTilePix / job.tile_width : 0;
+            }
+            if (job.big_tiles) c.big = job.big_tiles;
+            if (!c.valid() || c.big > gvr::kBigTiles)
+                rc = fail(GVR_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) +
+                                                        ": tile_width must be 8, 16 or 32 and big_tiles 1..16");
+            p->tiles[j] = c;
+        } else {
+            rc = tile_config_for(job.handle, &job.forward, (flags & GVR_PLAN_AUTOTUNE) != 0, p->tiles[j]);
+        }
+        if (rc != GVR_OK) {
+            delete p;
+            return rc;
+        }
+    }
+    // host copies of the tables
+    std::vector<int> start[gvr::kNumStages], items(count + 1, 0);
+    for (auto &s : start) s.assign(count + 1, 0);
+    long long totalItems = 0, totalBlocks[gvr::kNumStages] = {0};
+    for (int j = 0; j < count; ++j) {
+        const GvrHandle *h = jobs[j].handle;
+        const long long B = jobs[j].forward.batch, C = h->attrs.num_cameras;
+        const long long n[gvr::kNumStages] = {B * C, B * h->F, B * h->N, B * C * h->F, B * C * h->F};
+        for (int s = 0; s < gvr::kNumStages; ++s) {
+            start[s][j] = (int)totalBlocks[s];
+            totalBlocks[s] += (n[s] + gvr::kBatchBlock - 1) / gvr::kBatchBlock;
+        }
+        items[j] = (int)totalItems;
+        totalItems += B * C * p->tiles[j].tilesX(h) * p->tiles[j].tilesY(h);
+        if (totalItems >= INT_MAX || totalBlocks[gvr::kStageBinCount] >= INT_MAX) {
+            delete p;
+            return fail(GVR_ERR_INVALID_ARGUMENT, "plan too large for int32 indexing");
+        }
+    }
+    for (int s = 0; s < gvr::kNumStages; ++s) start[s][count] = (int)totalBlocks[s];
+    items[count] = (int)totalItems;
+
+    std::vector<FwdLayout> lay;
+    PlanTables t{};
+    size_t z0 = 0, z1 = 0;
+    const size_t bytes = plan_carve(*p, nullptr, lay, t, z0, z1);
+    cudaError_t e = cudaMalloc(&p->d_mem, bytes);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "cudaMalloc(plan)");
+    }
+    plan_carve(*p, p->d_mem, lay, t, z0, z1);
+    std::vector<gvr::FwdJob> hostJobs(count);
+    for (int j = 0; j < count; ++j) {
+        const GvrJob &job = jobs[j];
+        int Ht, Wt;
+        forward_texture_size(job.handle, &job.forward, Ht, Wt);
+        hostJobs[j] = make_job(job.handle, &job.forward, lay[j], dims_of(job.handle, job.forward.batch, Ht, Wt, p->tiles[j]));
+    }
+    e = cudaMemcpy(t.jobs, hostJobs.data(), sizeof(gvr::FwdJob) * count, cudaMemcpyHostToDevice);
+    for (int s = 0; s < gvr::kNumStages && e == cudaSuccess; ++s)
+        e = cudaMemcpy(t.blockStart[s], start[s].data(), sizeof(int) * (count + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t.itemStart, items.data(), sizeof(int) * (count + 1), cudaMemcpyHostToDevice);
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        gvr_plan_destroy(p);
+        return cuda_fail(e, "plan setup");
+    }
+    gvr::BatchLaunch &L = p->launch;
+    L.jobs = t.jobs;
+    for (int s = 0; s < gvr::kNumStages; ++s) {
+        L.blockStart[s] = t.blockStart[s];
+        L.blocks[s] = (int)totalBlocks[s];
+    }
+    L.itemStart = t.itemStart;
+    L.counter = t.counter;
+    L.nJobs = count;
+    L.rasterGrid = (int)std::min<long long>((long long)sms * gvr::raster_persistent_blocks_per_sm(), totalItems);
+    L.zeroBase = static_cast<char *>(p->d_mem) + z0;
+    L.zeroBytes = z1 - z0;
+    *out_plan = p;
+    return GVR_OK;
+}
+
+int gvr_plan_forward(GvrPlan *p, void *stream) {
+    if (!p) return fail(GVR_ERR_INVALID_ARGUMENT, "plan is NULL");
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    return plan_forward_body(p, static_cast<cudaStream_t>(stream));
+}
+
+int gvr_plan_forward_graph(GvrPlan *p, void *stream) {
+    if (!p) return fail(GVR_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!stream) return fail(GVR_ERR_INVALID_ARGUMENT, "graph capture needs a created (non-default) stream");
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!p->exec) {
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+        const int rc = plan_forward_body(p, st);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(st, &graph);
+        if (rc != GVR_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&p->exec, graph, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            p->exec = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+        p->graph = graph;
+    }
+    const cudaError_t e = cudaGraphLaunch(p->exec, st);
+    return e == cudaSuccess ? GVR_OK : cuda_fail(e, "cudaGraphLaunch");
+}
+
+int gvr_plan_tile_config(const GvrPlan *p, int32_t job, int32_t *tile_w, int32_t *tile_h, int32_t *big_tiles) {
+    if (!p || job < 0 || job >= (int)p->tiles.size()) return fail(GVR_ERR_INVALID_ARGUMENT, "bad plan or job index");
+    if (tile_w) *tile_w = p->tiles[job].w;
+    if (tile_h) *tile_h = p->tiles[job].h;
+    if (big_tiles) *big_tiles = p->tiles[job].big;
+    return GVR_OK;
+}
+
+void gvr_plan_destroy(GvrPlan *p) {
+    if (!p) return;
+    DeviceGuard g(p->device);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->d_mem) cudaFree(p->d_mem);
+    delete p;
+}
+
+}  // extern "C"

@@ -11,7 +11,12 @@
 //                 constants, per-tile counts                     B*C*F threads
 //   k_scan_tiles  exclusive scan of the tile counts              1 block
 //   k_bin_fill    per-tile face lists                            B*C*F threads
-//   k_raster      one 16x16 tile per block (replaces :215-408)
+//   k_raster      one tile per block (replaces :215-408)
+//
+// Each stage is a per-item device function of a FwdJob.  The *_batched
+// kernels run the same functions over many jobs (meshes of different sizes,
+// modes and resolutions) in one launch per stage: blockStart[j] is the
+// first block of job j, so every block belongs to one job.
 #include "gvr_internal.cuh"
 #include "gvr_kernels.h"
 #include "gvr_profile.h"
@@ -75,10 +80,8 @@ __device__ static void mat4_inverse_x(const float *e, float *out) {
     for (int i = 0; i < 16; ++i) out[i] = xm(inv[i], detr);
 }
 
-__global__ void k_cameras(const float *__restrict__ extr, const float *__restrict__ intr, Camera *__restrict__ cams,
-                          int count) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
+__device__ __forceinline__ void camera_item(const float *__restrict__ extr, const float *__restrict__ intr,
+                                            Camera *__restrict__ cams, int i) {
     const float *e12 = extr + 12 * (size_t)i, *k9 = intr + 9 * (size_t)i;
     float E[16], K[16], KE[16];
 #pragma unroll
@@ -114,10 +117,9 @@ __global__ void k_cameras(const float *__restrict__ extr, const float *__restric
 
 // ---------------------------------------------------------------------------- face setup
 
-__global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__restrict__ faces, FaceGeo *__restrict__ geo,
-                           float4 *__restrict__ fnormal, int N, int F, int B) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= B * F) return;
+__device__ __forceinline__ void face_geo_item(const float *__restrict__ verts, const int32_t *__restrict__ faces,
+                                              FaceGeo *__restrict__ geo, float4 *__restrict__ fnormal, int N, int F,
+                                              int i) {
     int b = i / F, f = i - b * F;
     const float *V = verts + (size_t)b * N * 3;
     int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
@@ -139,30 +141,27 @@ __global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__res
 
 // ---------------------------------------------------------------------------- vertex stage
 
-__global__ void k_vertices(const float *__restrict__ verts, const Topology topo, const float4 *__restrict__ fnormal,
-                           const Camera *__restrict__ cams, float *__restrict__ vnormal_out, float4 *__restrict__ proj,
-                           int B, int C) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int N = topo.N, F = topo.F;
-    if (i >= B * N) return;
+__device__ __forceinline__ void vertex_item(const FwdJob &J, int i) {
+    const Topology &topo = J.topo;
+    const int N = topo.N, F = topo.F, C = J.dims.C;
     int b = i / N, v = i - b * N;
     // vertex normal = sum of adjacent face normals in ascending face order
     V3 acc = v3(0.0f, 0.0f, 0.0f);
     int s = topo.vstart[v], e = topo.vstart[v + 1];
     for (int k = s; k < e; ++k) {
-        float4 n = fnormal[(size_t)b * F + topo.vfaces[k]];
+        float4 n = J.ws.fnormal[(size_t)b * F + topo.vfaces[k]];
         if (k == s) acc = v3(n.x, n.y, n.z);
         else acc = v3(xa(acc.x, n.x), xa(acc.y, n.y), xa(acc.z, n.z));
     }
-    V3 p = ld3(verts + (size_t)i * 3);
+    V3 p = ld3(J.io.verts + (size_t)i * 3);
     for (int c = 0; c < C; ++c) {
         size_t o = ((size_t)b * C + c) * N + v;
-        float *dst = vnormal_out + o * 3;
+        float *dst = J.vnormal_out + o * 3;
         dst[0] = acc.x;
         dst[1] = acc.y;
         dst[2] = acc.z;
         // getCamSpacePoint + projectPointFloat3 (CameraUtil.h:141-186)
-        const Camera &cam = cams[b * C + c];
+        const Camera &cam = J.ws.cams[b * C + c];
         const float *E = cam.E, *K = cam.K;
         float cx = xa(xa(xa(xm(E[0], p.x), xm(E[1], p.y)), xm(E[2], p.z)), xm(E[3], 1.0f));
         float cy = xa(xa(xa(xm(E[4], p.x), xm(E[5], p.y)), xm(E[6], p.z)), xm(E[7], 1.0f));
@@ -178,7 +177,7 @@ __global__ void k_vertices(const float *__restrict__ verts, const Topology topo,
             x = xd(x, z);
             y = xd(y, z);
         }
-        proj[o] = make_float4(x, y, z, 0.0f);
+        J.proj[o] = make_float4(x, y, z, 0.0f);
     }
 }
 
@@ -195,14 +194,14 @@ __device__ __forceinline__ int4 face_box(float4 p0, float4 p1, float4 p2, int W,
     return r;
 }
 
-__global__ void k_bin_count(const Topology topo, const float *__restrict__ verts, const float4 *__restrict__ proj,
-                            FrameDims dims, FwdScratch ws) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
+    const Topology &topo = J.topo;
+    const FrameDims &dims = J.dims;
+    const FwdScratch &ws = J.ws;
     const int F = topo.F, N = topo.N;
-    if (i >= dims.B * dims.C * F) return;
     int bc = i / F, f = i - bc * F, b = bc / dims.C;
     const int i0 = topo.faces[3 * f], i1 = topo.faces[3 * f + 1], i2 = topo.faces[3 * f + 2];
-    const float4 *P = proj + (size_t)bc * N;
+    const float4 *P = J.proj + (size_t)bc * N;
     float4 p0 = P[i0], p1 = P[i1], p2 = P[i2];
     int4 box = face_box(p0, p1, p2, dims.W, dims.H);
     if (box.x > box.z || box.y > box.w) box = make_int4(1, 1, 0, 0);
@@ -210,7 +209,7 @@ __global__ void k_bin_count(const Topology topo, const float *__restrict__ verts
     const float ex1 = p1.x - p0.x, ey1 = p1.y - p0.y, ex2 = p2.x - p0.x, ey2 = p2.y - p0.y;
     const float det = ex1 * ey2 - ey1 * ex2;
     const float zmn = fminf(p0.z, fminf(p1.z, p2.z)), zmx = fmaxf(p0.z, fmaxf(p1.z, p2.z));
-    const float *V = verts + (size_t)b * N * 3;
+    const float *V = J.io.verts + (size_t)b * N * 3;
     const Camera &cam = ws.cams[bc];
     const float4 fn = ws.fnormal[(size_t)b * F + f];
     const V3 w0 = ld3(V + 3 * i0), w1 = ld3(V + 3 * i1), w2 = ld3(V + 3 * i2);
@@ -257,10 +256,11 @@ __global__ void k_bin_count(const Topology topo, const float *__restrict__ verts
     vf.s1 = s1;
     ws.vface[i] = vf;
     if (box.x > box.z || box.y > box.w) return;
-    int tx0 = box.x / kTile, tx1 = box.z / kTile, ty0 = box.y / kTile, ty1 = box.w / kTile;
+    const int sh = dims.tileShift, tH = dims.tileH;
+    int tx0 = box.x >> sh, tx1 = box.z >> sh, ty0 = box.y / tH, ty1 = box.w / tH;
     int nt = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
     const int T = dims.tilesX * dims.tilesY;
-    if (nt > kBigTiles) {
+    if (nt > dims.bigTiles) {
         int k = atomicAdd(&ws.bigCount[bc], 1);
         ws.bigList[(size_t)bc * F + k] = f;
         return;
@@ -270,8 +270,8 @@ __global__ void k_bin_count(const Topology topo, const float *__restrict__ verts
         for (int tx = tx0; tx <= tx1; ++tx) atomicAdd(&cnt[ty * dims.tilesX + tx], 1);
 }
 
-// Exclusive scan of n counts by one 1024-thread block.
-__global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ count, int *__restrict__ start, int n) {
+// Exclusive scan of n counts by one 1024-thread block; start[n] = total.
+__device__ __forceinline__ void scan_block(const int *__restrict__ count, int *__restrict__ start, int n) {
     __shared__ int warpSum[32];
     __shared__ int carry;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -308,15 +308,16 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ cou
     if (tid == 0) start[n] = carry;
 }
 
-__global__ void k_bin_fill(const Topology topo, FrameDims dims, FwdScratch ws) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int F = topo.F;
-    if (i >= dims.B * dims.C * F) return;
+__device__ __forceinline__ void bin_fill_item(const FwdJob &J, int i) {
+    const FrameDims &dims = J.dims;
+    const FwdScratch &ws = J.ws;
+    const int F = J.topo.F;
     int bc = i / F, f = i - bc * F;
     int4 box = vf_box(ws.vface[i]);
     if (box.x > box.z || box.y > box.w) return;
-    int tx0 = box.x / kTile, tx1 = box.z / kTile, ty0 = box.y / kTile, ty1 = box.w / kTile;
-    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > kBigTiles) return;
+    const int sh = dims.tileShift, tH = dims.tileH;
+    int tx0 = box.x >> sh, tx1 = box.z >> sh, ty0 = box.y / tH, ty1 = box.w / tH;
+    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > dims.bigTiles) return;
     const int T = dims.tilesX * dims.tilesY;
     for (int ty = ty0; ty <= ty1; ++ty)
         for (int tx = tx0; tx <= tx1; ++tx) {
@@ -324,6 +325,81 @@ __global__ void k_bin_fill(const Topology topo, FrameDims dims, FwdScratch ws) {
             int pos = atomicAdd(&ws.tileCursor[t], 1);
             ws.bins[ws.tileStart[t] + pos] = f;
         }
+}
+
+// ---------------------------------------------------------------------------- single-call kernels
+
+__global__ void k_cameras(const float *__restrict__ extr, const float *__restrict__ intr, Camera *__restrict__ cams,
+                          int count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) camera_item(extr, intr, cams, i);
+}
+
+__global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__restrict__ faces, FaceGeo *__restrict__ geo,
+                           float4 *__restrict__ fnormal, int N, int F, int B) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < B * F) face_geo_item(verts, faces, geo, fnormal, N, F, i);
+}
+
+__global__ void k_vertices(const FwdJob J) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < J.dims.B * J.topo.N) vertex_item(J, i);
+}
+
+__global__ void k_bin_count(const FwdJob J) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < J.dims.B * J.dims.C * J.topo.F) bin_count_item(J, i);
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ count, int *__restrict__ start, int n) {
+    scan_block(count, start, n);
+}
+
+__global__ void k_bin_fill(const FwdJob J) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < J.dims.B * J.dims.C * J.topo.F) bin_fill_item(J, i);
+}
+
+// ---------------------------------------------------------------------------- batched kernels
+
+// The job owning block `blk`: the last j with blockStart[j] <= blk.
+__device__ __forceinline__ int job_of_block(const int *__restrict__ blockStart, int nJobs, int blk) {
+    int lo = 0, hi = nJobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (blockStart[mid] <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Index spaces of the batched stages (BatchStage) and their per-job counts.
+__device__ __forceinline__ int stage_count(const FwdJob &J, int stage) {
+    switch (stage) {
+        case kStageViews: return J.dims.B * J.dims.C;
+        case kStageFaces: return J.dims.B * J.topo.F;
+        case kStageVertices: return J.dims.B * J.topo.N;
+        default: return J.dims.B * J.dims.C * J.topo.F;
+    }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kBatchBlock) k_stage_batched(const FwdJob *__restrict__ jobs,
+                                                               const int *__restrict__ blockStart, int nJobs) {
+    const int j = job_of_block(blockStart, nJobs, blockIdx.x);
+    const FwdJob &J = jobs[j];
+    const int i = (blockIdx.x - blockStart[j]) * kBatchBlock + threadIdx.x;
+    if (i >= stage_count(J, STAGE)) return;
+    if (STAGE == kStageViews) camera_item(J.extr, J.intr, J.ws.cams, i);
+    else if (STAGE == kStageFaces) face_geo_item(J.io.verts, J.topo.faces, J.ws.geo, J.ws.fnormal, J.topo.N, J.topo.F, i);
+    else if (STAGE == kStageVertices) vertex_item(J, i);
+    else if (STAGE == kStageBinCount) bin_count_item(J, i);
+    else bin_fill_item(J, i);
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles_batched(const FwdJob *__restrict__ jobs) {
+    const FwdJob &J = jobs[blockIdx.x];
+    scan_block(J.ws.tileCount, J.ws.tileStart, J.dims.B * J.dims.C * J.dims.tilesX * J.dims.tilesY);
 }
 
 // ---------------------------------------------------------------------------- host launch
@@ -343,28 +419,71 @@ cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *g
     return cudaGetLastError();
 }
 
-cudaError_t launch_forward(const Topology &topo, const FrameDims &dims, const FwdScratch &ws, const float *verts,
-                           const float *colors, const float *texture, const float *sh, const float *extr,
-                           const float *intr, float *bary, int32_t *face, float *render, float *vnormal,
-                           float4 *proj, cudaStream_t st) {
+static cudaError_t launch_vertices(const FwdJob &J, cudaStream_t st) {
+    GVR_LAUNCH(st, "k_vertices", k_vertices<<<blocks((size_t)J.dims.B * J.topo.N, 256), 256, 0, st>>>(J));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
+    const FrameDims &dims = J.dims;
     const int B = dims.B, C = dims.C, T = dims.tilesX * dims.tilesY;
-    cudaError_t err = cudaMemsetAsync(ws.zeroBase, 0, ws.zeroBytes, st);
+    cudaError_t err = cudaMemsetAsync(J.ws.zeroBase, 0, J.ws.zeroBytes, st);
     if (err != cudaSuccess) return err;
-    if ((err = launch_cameras(extr, intr, ws.cams, B * C, st)) != cudaSuccess) return err;
-    if ((err = launch_face_geo(verts, topo, ws.geo, ws.fnormal, B, st)) != cudaSuccess) return err;
-    GVR_LAUNCH(st, "k_vertices",
-               k_vertices<<<blocks((size_t)B * topo.N, 256), 256, 0, st>>>(verts, topo, ws.fnormal, ws.cams, vnormal,
-                                                                            proj, B, C));
+    if ((err = launch_cameras(J.extr, J.intr, J.ws.cams, B * C, st)) != cudaSuccess) return err;
+    if ((err = launch_face_geo(J.io.verts, J.topo, J.ws.geo, J.ws.fnormal, B, st)) != cudaSuccess) return err;
+    if ((err = launch_vertices(J, st)) != cudaSuccess) return err;
+    const size_t nvf = (size_t)B * C * J.topo.F;
+    GVR_LAUNCH(st, "k_bin_count", k_bin_count<<<blocks(nvf, 256), 256, 0, st>>>(J));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    const size_t nvf = (size_t)B * C * topo.F;
-    GVR_LAUNCH(st, "k_bin_count", k_bin_count<<<blocks(nvf, 256), 256, 0, st>>>(topo, verts, proj, dims, ws));
+    GVR_LAUNCH(st, "k_scan_tiles", k_scan_tiles<<<1, 1024, 0, st>>>(J.ws.tileCount, J.ws.tileStart, B * C * T));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    GVR_LAUNCH(st, "k_scan_tiles", k_scan_tiles<<<1, 1024, 0, st>>>(ws.tileCount, ws.tileStart, B * C * T));
+    GVR_LAUNCH(st, "k_bin_fill", k_bin_fill<<<blocks(nvf, 256), 256, 0, st>>>(J));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    GVR_LAUNCH(st, "k_bin_fill", k_bin_fill<<<blocks(nvf, 256), 256, 0, st>>>(topo, dims, ws));
+    return launch_raster(J, st);
+}
+
+// compute_normal_map: cameras, vertex normals and projections as above, then
+// the texture-space normal map instead of the depth and shading passes
+// (renderBuffersGPU, CUDABasedRasterization.cu:449-473).
+cudaError_t launch_forward_normal_map(const FwdJob &J, int *uvOwner, float *normal_map, cudaStream_t st) {
+    const int B = J.dims.B, C = J.dims.C;
+    cudaError_t err;
+    if ((err = launch_cameras(J.extr, J.intr, J.ws.cams, B * C, st)) != cudaSuccess) return err;
+    if ((err = launch_face_geo(J.io.verts, J.topo, J.ws.geo, J.ws.fnormal, B, st)) != cudaSuccess) return err;
+    if ((err = launch_vertices(J, st)) != cudaSuccess) return err;
+    return launch_normal_map(J.topo, J.dims, uvOwner, J.vnormal_out, normal_map, J.io.face, J.io.bary, J.io.render,
+                             st);
+}
+
+// The batched forward of many jobs: one launch per stage over all jobs, then
+// the persistent raster.  blockStart[s] holds nJobs + 1 block offsets of
+// stage s (kBatchBlock threads per block); itemStart the raster items.
+cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st) {
+    cudaError_t err = cudaMemsetAsync(L.zeroBase, 0, L.zeroBytes, st);
+    if (err != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_cameras_batched",
+               k_stage_batched<kStageViews><<<L.blocks[kStageViews], kBatchBlock, 0, st>>>(
+                   L.jobs, L.blockStart[kStageViews], L.nJobs));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    RasterIO io{verts, colors, texture, sh, vnormal, bary, face, render};
-    return launch_raster(topo, dims, ws, io, st);
+    GVR_LAUNCH(st, "k_face_geo_batched",
+               k_stage_batched<kStageFaces><<<L.blocks[kStageFaces], kBatchBlock, 0, st>>>(
+                   L.jobs, L.blockStart[kStageFaces], L.nJobs));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_vertices_batched",
+               k_stage_batched<kStageVertices><<<L.blocks[kStageVertices], kBatchBlock, 0, st>>>(
+                   L.jobs, L.blockStart[kStageVertices], L.nJobs));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_bin_count_batched",
+               k_stage_batched<kStageBinCount><<<L.blocks[kStageBinCount], kBatchBlock, 0, st>>>(
+                   L.jobs, L.blockStart[kStageBinCount], L.nJobs));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_scan_tiles_batched", k_scan_tiles_batched<<<L.nJobs, 1024, 0, st>>>(L.jobs));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_bin_fill_batched",
+               k_stage_batched<kStageBinFill><<<L.blocks[kStageBinCount], kBatchBlock, 0, st>>>(
+                   L.jobs, L.blockStart[kStageBinCount], L.nJobs));
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    return launch_raster_persistent(L.jobs, L.itemStart, L.nJobs, L.counter, L.rasterGrid, st);
 }
 
 // Per-pixel rays for tests (same pixel_ray as the raster).

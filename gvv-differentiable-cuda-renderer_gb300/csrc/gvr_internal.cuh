@@ -255,9 +255,15 @@ struct Topology {
     int N, F;
 };
 
+// Per-call frame description.  The forward bins faces into tiles of
+// tileW x tileH = 256 pixels (tileW in {8, 16, 32}; default 16 x 16) and
+// sends faces spanning more than bigTiles tiles to a per-view list that
+// every tile scans; tilesX/tilesY count those tiles.  The backward always
+// works on 16 x 16 tiles.
 struct FrameDims {
     int B, C, W, H, tilesX, tilesY, Ht, Wt;
     int albedo, shading;
+    int tileW, tileH, tileShift, bigTiles;  // tileShift = log2(tileW)
 };
 
 // Forward scratch carved out of one workspace.
@@ -286,6 +292,20 @@ struct RasterIO {
     float *bary;             // [B,C,H,W,2]
     int32_t *face;           // [B,C,H,W]
     float *render;           // [B,C,H,W,3]
+};
+
+// One forward job: one handle's topology and one call's frame, scratch and
+// buffers.  The single-mesh kernels take it by value; the batched kernels
+// read an array of them from device memory.
+struct FwdJob {
+    Topology topo;
+    FrameDims dims;
+    FwdScratch ws;
+    RasterIO io;
+    const float *extr;   // [B,C,12]
+    const float *intr;   // [B,C,9]
+    float4 *proj;        // [B*C*N] projected vertices
+    float *vnormal_out;  // [B,C,N,3] (the buffer io.vnormal reads)
 };
 
 struct BwdScratch {

@@ -60,6 +60,9 @@ KernelScope::KernelScope(cudaStream_t st, const char *name) : st_(st), name_(nam
     g_launches.fetch_add(1, std::memory_order_relaxed);
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_enabled) return;
+    // no timing inside a stream capture: the launch becomes a graph node
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st_, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return;
     a_ = take_event();
     b_ = take_event();
     if (a_ && b_) cudaEventRecord(a_, st_);

@@ -1,5 +1,6 @@
-// gvr_raster.cu -- visibility, resolve and shading of one 16x16 pixel tile
-// per block (the work of renderDepthBufferDevice + renderBuffersDevice,
+// gvr_raster.cu -- visibility, resolve and shading of one 256-pixel tile
+// (16x16 by default; 32x8 or 8x32 when a batched plan picks them) per block
+// (the work of renderDepthBufferDevice + renderBuffersDevice,
 // cpp/src/Renderer/CUDABasedRasterization.cu:215-408).
 //
 // The reference tests every pixel of every face's box with its FP32
@@ -42,7 +43,7 @@ struct __align__(16) Entry {
     int bx0, by0, bx1, by1;
 };
 
-__device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX0, int tileY0) {
+__device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX0, int tileY0, int tileW, int tileH) {
     Entry E;
     E.x0 = vf.s0.x;
     E.y0 = vf.s0.y;
@@ -63,8 +64,8 @@ __device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX
     const int4 box = vf_box(vf);
     E.bx0 = max(box.x, tileX0);
     E.by0 = max(box.y, tileY0);
-    E.bx1 = min(box.z, tileX0 + kTile - 1);
-    E.by1 = min(box.w, tileY0 + kTile - 1);
+    E.bx1 = min(box.z, tileX0 + tileW - 1);
+    E.by1 = min(box.w, tileY0 + tileH - 1);
     return E;
 }
 
@@ -127,16 +128,22 @@ __device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f
     return depth_key(depth_quantised(abc, z.x, z.y, z.z), f);
 }
 
-}  // namespace
-
-__global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameDims dims, FwdScratch ws, RasterIO io) {
+// One tile of one view: item = bc * tiles + tile of job J (256 threads, one
+// pixel each).  Shared by the per-call grid kernel and the persistent
+// batched kernel, so both produce the same bits.
+__device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
+    const Topology &topo = J.topo;
+    const FrameDims &dims = J.dims;
+    const FwdScratch &ws = J.ws;
+    const RasterIO &io = J.io;
     __shared__ Entry sE[kCachedEntries];
     __shared__ int sCount;
     const int T = dims.tilesX * dims.tilesY;
-    const int tile = blockIdx.x % T, bc = blockIdx.x / T, b = bc / dims.C;
-    const int tileX0 = (tile % dims.tilesX) * kTile, tileY0 = (tile / dims.tilesX) * kTile;
+    const int tile = item % T, bc = item / T, b = bc / dims.C;
+    const int tileW = dims.tileW, tileH = dims.tileH;
+    const int tileX0 = (tile % dims.tilesX) * tileW, tileY0 = (tile / dims.tilesX) * tileH;
     const int tid = threadIdx.x;
-    const int u = tileX0 + (tid & (kTile - 1)), v = tileY0 + tid / kTile;
+    const int u = tileX0 + (tid & (tileW - 1)), v = tileY0 + (tid >> dims.tileShift);
     const float px = u + 0.5f, py = v + 0.5f;
     const int F = topo.F;
     const ViewFace *VF = ws.vface + (size_t)bc * F;
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
         Entry E;
         if (e < nAll) {
             const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
-            E = make_entry(VF[f], f, tileX0, tileY0);
+            E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
             keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -174,7 +181,8 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     __syncthreads();
     const int nE = sCount;
     const bool overflow = nE > kCachedEntries;  // block-uniform: then walk the global list instead
-    const int rowLo = tileY0 + 2 * (tid >> 5), rowHi = rowLo + 1;  // the two rows of this warp
+    // the pixel rows of this warp (32 / tileW rows of tileW pixels)
+    const int rowLo = tileY0 + ((tid & ~31) >> dims.tileShift), rowHi = rowLo + (32 >> dims.tileShift) - 1;
 
     // Front-to-back order: counting sort into kBuckets depth buckets spanning
     // the tile's finite depth lower bounds (faces without a bound go first).
@@ -207,13 +215,21 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
         };
         for (int e = tid; e < nE; e += kTilePix) atomicAdd(&sHist[bucket_of(sKey[e])], 1);
         __syncthreads();
-        if (tid == 0) {
-            int run = 0;
-            for (int q = 0; q <= kBuckets; ++q) {
-                const int c = sHist[q];
-                sHist[q] = run;
-                run += c;
+        if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: 3 per lane, one warp scan
+            const int q0 = 3 * tid;
+            const int c0 = q0 <= kBuckets ? sHist[q0] : 0, c1 = q0 + 1 <= kBuckets ? sHist[q0 + 1] : 0,
+                      c2 = q0 + 2 <= kBuckets ? sHist[q0 + 2] : 0;
+            const int own = c0 + c1 + c2;
+            int incl = own;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (tid >= o) incl += y;
             }
+            const int ex = incl - own;
+            if (q0 <= kBuckets) sHist[q0] = ex;
+            if (q0 + 1 <= kBuckets) sHist[q0 + 1] = ex + c0;
+            if (q0 + 2 <= kBuckets) sHist[q0 + 2] = ex + c0 + c1;
         }
         __syncthreads();
         for (int e = tid; e < nE; e += kTilePix) {
@@ -233,7 +249,7 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
             return true;
         }
         const int f = i < nTile ? ws.bins[s0 + i] : bigList[i - nTile];
-        E = make_entry(VF[f], f, tileX0, tileY0);
+        E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
         return E.bx0 <= E.bx1 && E.by0 <= E.by1;
     };
     const int nWalk = overflow ? nAll : nE;
@@ -405,11 +421,66 @@ __global__ void __launch_bounds__(kTilePix) k_raster(const Topology topo, FrameD
     io.render[3 * p + 2] = col.z;
 }
 
-cudaError_t launch_raster(const Topology &topo, const FrameDims &dims, const FwdScratch &ws, const RasterIO &io,
-                          cudaStream_t st) {
-    const int grid = dims.B * dims.C * dims.tilesX * dims.tilesY;
-    GVR_LAUNCH(st, "k_raster", k_raster<<<grid, kTilePix, 0, st>>>(topo, dims, ws, io));
+}  // namespace
+
+// One block per tile of one call.
+__global__ void __launch_bounds__(kTilePix) k_raster(const FwdJob J) { raster_tile(J, blockIdx.x); }
+
+// Persistent: a grid sized to the resident capacity pulls (job, view, tile)
+// items from one counter until all jobs' tiles are done.  itemStart[j] is the
+// first item of job j (exclusive prefix of its B*C*tiles).
+__global__ void __launch_bounds__(kTilePix, 3) k_raster_persistent(const FwdJob *__restrict__ jobs,
+                                                                const int *__restrict__ itemStart, int nJobs,
+                                                                int *__restrict__ counter) {
+    __shared__ int sItem, sJob;
+    __shared__ FwdJob sJ;
+    const int total = itemStart[nJobs];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int item = atomicAdd(counter, 1);
+            int j = 0;
+            if (item < total) {
+                int lo = 0, hi = nJobs - 1;  // last job whose first item is <= item
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (itemStart[mid] <= item) lo = mid;
+                    else hi = mid - 1;
+                }
+                j = lo;
+            }
+            sItem = item;
+            sJob = j;
+        }
+        __syncthreads();
+        const int item = sItem, j = sJob;
+        if (item >= total) break;
+        // the job record, staged once per item for uniform shared-memory reads
+        const int words = (int)(sizeof(FwdJob) / sizeof(int));
+        for (int w = threadIdx.x; w < words; w += blockDim.x)
+            reinterpret_cast<int *>(&sJ)[w] = reinterpret_cast<const int *>(jobs + j)[w];
+        __syncthreads();
+        raster_tile(sJ, item - itemStart[j]);
+        __syncthreads();  // shared memory and sItem are reused by the next item
+    }
+}
+
+cudaError_t launch_raster(const FwdJob &J, cudaStream_t st) {
+    const int grid = J.dims.B * J.dims.C * J.dims.tilesX * J.dims.tilesY;
+    GVR_LAUNCH(st, "k_raster", k_raster<<<grid, kTilePix, 0, st>>>(J));
     return cudaGetLastError();
+}
+
+cudaError_t launch_raster_persistent(const FwdJob *jobs, const int *itemStart, int nJobs, int *counter, int grid,
+                                     cudaStream_t st) {
+    GVR_LAUNCH(st, "k_raster_persistent",
+               k_raster_persistent<<<grid, kTilePix, 0, st>>>(jobs, itemStart, nJobs, counter));
+    return cudaGetLastError();
+}
+
+int raster_persistent_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster_persistent, kTilePix, 0) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
 }
 
 }  // namespace gvr

@@ -44,6 +44,13 @@ class GvrBackwardArgs(ctypes.Structure):
                 ("workspace", P), ("workspace_bytes", ctypes.c_size_t)]
 
 
+class GvrJob(ctypes.Structure):
+    _fields_ = [("handle", P), ("forward", GvrForwardArgs), ("tile_width", I32), ("big_tiles", I32)]
+
+
+PLAN_AUTOTUNE = 1
+
+
 class GvrKernelTime(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_longlong), ("total_ms", ctypes.c_double)]
 
@@ -51,7 +58,9 @@ class GvrKernelTime(ctypes.Structure):
 # Every symbol include/gvr.h declares.
 EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forward_workspace_size",
            "gvr_backward_workspace_size", "gvr_last_error", "gvr_abi_version", "gvr_debug_rays",
-           "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc")
+           "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc",
+           "gvr_plan_create", "gvr_plan_forward", "gvr_plan_forward_graph", "gvr_plan_tile_config",
+           "gvr_plan_destroy")
 
 NOALLOC_SCRATCH_BYTES = 32 << 20  # GVR_NOALLOC_SCRATCH_BYTES
 
@@ -94,6 +103,17 @@ def load(build_if_missing: bool = True):
     L.gvr_launch_count.restype = ctypes.c_longlong
     L.gvr_backward_noalloc.argtypes = [P, ctypes.POINTER(GvrBackwardArgs), P]
     L.gvr_backward_noalloc.restype = ctypes.c_int
+    L.gvr_plan_create.argtypes = [ctypes.POINTER(GvrJob), I32, I32, ctypes.POINTER(P)]
+    L.gvr_plan_create.restype = ctypes.c_int
+    L.gvr_plan_forward.argtypes = [P, P]
+    L.gvr_plan_forward.restype = ctypes.c_int
+    L.gvr_plan_forward_graph.argtypes = [P, P]
+    L.gvr_plan_forward_graph.restype = ctypes.c_int
+    I32P = ctypes.POINTER(I32)
+    L.gvr_plan_tile_config.argtypes = [P, I32, I32P, I32P, I32P]
+    L.gvr_plan_tile_config.restype = ctypes.c_int
+    L.gvr_plan_destroy.argtypes = [P]
+    L.gvr_plan_destroy.restype = None
     _lib = L
     return L
 

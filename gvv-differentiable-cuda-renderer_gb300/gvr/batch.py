@@ -1,0 +1,96 @@
+"""Batched forward of many meshes through one plan (gvr_plan_* in include/gvr.h).
+
+The reference renders one mesh per op call and loops over the batch on the
+host (cpp/src/TensorflowOperators/CudaRenderer/CudaRenderer.cpp:309).  A
+BatchPlan binds many jobs -- each a RendererHandle (mesh, views, resolution,
+modes) with its own inputs -- once, and renders them all with one launch per
+pipeline stage and one persistent raster kernel, optionally replayed as a
+captured CUDA graph.  Each job's outputs equal render_forward's bit for bit.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .renderer import RendererHandle, _as_f32
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class BatchPlan:
+    """jobs: list of dicts with keys handle (RendererHandle), vertex_pos
+    [B,N,3], vertex_color [B,N,3] (vertexColor mode), texture [B,Ht,Wt,3]
+    (textured mode), sh_coeff [B,C,27], extrinsics [B,C,12], intrinsics
+    [B,C,9], and optionally tile_width (8/16/32) and big_tiles (1..16) to fix
+    the bin/tile configuration.  Inputs are copied to contiguous float32
+    device tensors owned by the plan; update them in place (plan.inputs[j])
+    between calls.  Outputs live in plan.outputs[j]."""
+
+    def __init__(self, jobs, autotune=False):
+        if not jobs:
+            raise ValueError("a plan needs at least one job")
+        self._L = _lib.load()
+        self.inputs, self.outputs, self.handles = [], [], []
+        arr = (_lib.GvrJob * len(jobs))()
+        for j, job in enumerate(jobs):
+            h: RendererHandle = job["handle"]
+            dev = h.device
+            B = int(job["vertex_pos"].shape[0])
+            vp = _as_f32(job["vertex_pos"], dev, (B, h.N, 3))
+            vc = _as_f32(job.get("vertex_color"), dev, (B, h.N, 3)) if job.get("vertex_color") is not None else None
+            tex = _as_f32(job.get("texture"), dev) if job.get("texture") is not None else None
+            sh = _as_f32(job["sh_coeff"], dev, (B, h.C, 27))
+            ex = _as_f32(job["extrinsics"], dev, (B, h.C, 12))
+            ix = _as_f32(job["intrinsics"], dev, (B, h.C, 9))
+            Ht, Wt = (int(tex.shape[1]), int(tex.shape[2])) if tex is not None else (1, 1)
+            out = dict(barycentric=torch.empty((B, h.C, h.H, h.W, 2), device=dev),
+                       face=torch.empty((B, h.C, h.H, h.W), dtype=torch.int32, device=dev),
+                       render=torch.empty((B, h.C, h.H, h.W, 3), device=dev),
+                       vertex_normal=torch.empty((B, h.C, h.N, 3), device=dev))
+            inp = dict(vertex_pos=vp, vertex_color=vc, texture=tex, sh_coeff=sh, extrinsics=ex, intrinsics=ix)
+            arr[j].handle = h.ptr
+            arr[j].forward = _lib.GvrForwardArgs(B, Ht, Wt, _ptr(vp), _ptr(vc), _ptr(tex), _ptr(sh), None, _ptr(ex),
+                                                 _ptr(ix), _ptr(out["barycentric"]), _ptr(out["face"]),
+                                                 _ptr(out["render"]), _ptr(out["vertex_normal"]), None, None, None, 0)
+            arr[j].tile_width = int(job.get("tile_width", 0))
+            arr[j].big_tiles = int(job.get("big_tiles", 0))
+            self.inputs.append(inp)
+            self.outputs.append(out)
+            self.handles.append(h)
+        self.device = self.handles[0].device
+        self._jobs = arr
+        plan = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self._L.gvr_plan_create(arr, len(jobs), _lib.PLAN_AUTOTUNE if autotune else 0,
+                                               ctypes.byref(plan)))
+        self._plan = plan
+
+    def forward(self, stream=None, graph=False):
+        """Renders every job on `stream` (default: torch's current stream).
+        graph=True captures the plan into a CUDA graph on the first call and
+        replays it afterwards (needs a non-default stream)."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        s = ctypes.c_void_p(st.cuda_stream)
+        fn = self._L.gvr_plan_forward_graph if graph else self._L.gvr_plan_forward
+        _lib.check(fn(self._plan, s))
+        return self.outputs
+
+    def tile_config(self, j):
+        w, h, b = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(self._L.gvr_plan_tile_config(self._plan, j, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b)))
+        return w.value, h.value, b.value
+
+    def close(self):
+        if getattr(self, "_plan", None) is not None and self._plan.value:
+            self._L.gvr_plan_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

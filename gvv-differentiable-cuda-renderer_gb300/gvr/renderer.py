@@ -81,8 +81,8 @@ class RendererHandle:
         except Exception:
             pass
 
-    def forward_workspace_size(self, batch):
-        return int(self._L.gvr_forward_workspace_size(self._h, batch, 0, 0))
+    def forward_workspace_size(self, batch, texture_height=0, texture_width=0):
+        return int(self._L.gvr_forward_workspace_size(self._h, batch, texture_height, texture_width))
 
     def backward_workspace_size(self, batch):
         return int(self._L.gvr_backward_workspace_size(self._h, batch, 0, 0))
@@ -155,12 +155,15 @@ def render_forward(h: RendererHandle, vertex_pos, vertex_color, texture, sh_coef
     img = torch.empty((B, h.C, h.H, h.W, 3), dtype=torch.float32, device=dev)
     vnorm = torch.empty((B, h.C, h.N, 3), dtype=torch.float32, device=dev)
     tout = torch.empty_like(tgt) if (copy_target and tgt is not None) else None
-    ws_bytes = h.forward_workspace_size(B)
+    # written by the forward with compute_normal_map; zeros otherwise (the
+    # reference leaves that output unwritten)
+    nmap = (torch.empty if h.compute_normal_map else torch.zeros)((B, Ht, Wt, 3), dtype=torch.float32, device=dev)
+    ws_bytes = h.forward_workspace_size(B, Ht, Wt)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     args = _lib.GvrForwardArgs(B, Ht, Wt, _ptr(vp), _ptr(vc), _ptr(tex), _ptr(sh), _ptr(tgt), _ptr(ex), _ptr(ix),
-                               _ptr(bary), _ptr(face), _ptr(img), _ptr(vnorm), _ptr(tout), None, _ptr(ws), ws_bytes)
+                               _ptr(bary), _ptr(face), _ptr(img), _ptr(vnorm), _ptr(tout),
+                               _ptr(nmap) if h.compute_normal_map else None, _ptr(ws), ws_bytes)
     _lib.check(h._L.gvr_forward(h.ptr, ctypes.byref(args), _stream(dev)))
-    nmap = torch.zeros((B, Ht, Wt, 3), dtype=torch.float32, device=dev)
     return bary, face, img, vnorm, (tout if tout is not None else tgt), nmap
 
 

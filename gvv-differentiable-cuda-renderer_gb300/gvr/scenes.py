@@ -218,6 +218,46 @@ def scene(num_faces, num_views, width, height, albedo_mode, shading_mode="shaded
     return out
 
 
+ALBEDO_MODES = ("vertexColor", "textured", "normal", "lighting", "foregroundMask")
+SHADING_MODES = ("shaded", "shadeless")
+
+
+def uneven_batch(seed=0, num_meshes=64, faces_range=(1000, 200000), max_views=8, resolutions=(256, 512, 1024),
+                 tex_size=512, sigma_mm=20.0):
+    """Batched uneven workload: `num_meshes` displaced spheres with face
+    counts log-uniform in `faces_range` (rounded to even), 1..max_views ring
+    views each, every view's resolution drawn from `resolutions`, albedo and
+    shading modes drawn from the reference's 5 x 2 set, textures
+    tex_size^2 U[0, 1].  The reference op renders all its cameras at one
+    resolution, so the views of a mesh that share a resolution form one job.
+    Returns a list of job dicts in scene()'s layout (batch 1) with the mesh
+    index under "mesh"."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(faces_range[0]), math.log(faces_range[1])
+    jobs = []
+    for m in range(num_meshes):
+        F = max(20, int(round(math.exp(rng.uniform(lo, hi)) / 2.0)) * 2)
+        views = int(rng.integers(1, max_views + 1))
+        res = rng.choice(np.asarray(resolutions), size=views)
+        albedo = ALBEDO_MODES[int(rng.integers(0, len(ALBEDO_MODES)))]
+        shading = SHADING_MODES[int(rng.integers(0, len(SHADING_MODES)))]
+        verts, faces, unit = displaced_sphere(F, 1000.0, sigma_mm, rng)
+        uvs = spherical_uvs(unit, faces)
+        N = verts.shape[0]
+        colors = rng.uniform(0, 1, size=(1, N, 3)).astype(np.float32)
+        texture = rng.uniform(0, 1, size=(1, tex_size, tex_size, 3)).astype(np.float32)
+        cams = ring_cameras(views, 3000.0, 15.0, rng, yaw0_deg=float(rng.uniform(0, 360)))
+        sh = sh_coefficients(views, rng)
+        for r in sorted(set(int(x) for x in res)):
+            sel = np.nonzero(res == r)[0]
+            C = len(sel)
+            jobs.append(dict(mesh=m, faces=faces, uvs=uvs, num_vertices=N, num_views=C, width=r, height=r,
+                             albedo_mode=albedo, shading_mode=shading, vertex_pos=verts[None], vertex_color=colors,
+                             texture=texture, sh_coeff=sh[sel][None], extrinsics=cams[sel][None],
+                             intrinsics=np.stack([intrinsics(r, r)] * C)[None]))
+    return jobs
+
+
 def single_view_vertex_color(seed=0):
     """Plain fwd+bwd: 2,562 V / 5,120 F displaced icosphere (sigma 20 mm),
     vertex colours, SH-shaded, one 256x256 view 3 m away, 40 deg FOV."""

@@ -74,7 +74,9 @@ typedef struct {
     int32_t shading_mode;         /* GvrShadingMode (foregroundMask forces shadeless) */
     int32_t image_filter_size;    /* >= 1, window half-size of the target-image gradient */
     int32_t texture_filter_size;  /* >= 1, accepted; unused by the reference kernels too */
-    int32_t compute_normal_map;   /* 0/1 */
+    int32_t compute_normal_map;   /* 1: write the texture-space normal map instead of
+                                     rendering; the frame outputs stay cleared (face -1,
+                                     barycentrics 0, green), as in the reference */
 } GvrAttrs;
 
 /* CudaRendererGpu inputs 0-6 and outputs 0-5 (CudaRenderer.cpp:7-20). */
@@ -94,7 +96,8 @@ typedef struct {
     float *render;                /* out [B,C,H,W,3]                            */
     float *vertex_normal;         /* out [B,C,N,3]                              */
     float *target_image_out;      /* out [B,C,H,W,3] copy of target_image, or NULL */
-    float *normal_map;            /* out [B,Ht,Wt,3] (compute_normal_map), or NULL */
+    float *normal_map;            /* out [B,Ht,Wt,3]; required with compute_normal_map,
+                                     otherwise NULL or cleared to 0 */
     void *workspace;              /* optional device scratch, >= gvr_forward_workspace_size */
     size_t workspace_bytes;
 } GvrForwardArgs;
@@ -176,6 +179,46 @@ int gvr_debug_rays(GvrHandle *handle, int32_t batch, const float *extrinsics, co
  * results; everything that must start at zero is cleared inside each call. */
 #define GVR_NOALLOC_SCRATCH_BYTES (32u << 20)
 int gvr_backward_noalloc(GvrHandle *handle, const GvrBackwardArgs *args, void *stream);
+
+/* ---- Batched forward of many meshes (no reference counterpart: the
+ * reference renders one mesh per op call and loops over the batch on the
+ * host, CudaRenderer.cpp:309).
+ *
+ * A plan binds a list of forward jobs -- each a handle (mesh topology,
+ * views, resolution, modes) with one call's device buffers -- once, and
+ * renders all of them with one launch per pipeline stage over every job
+ * and one persistent raster kernel that pulls (job, view, tile) items from
+ * a shared counter, so meshes of very different sizes share the GPU without
+ * per-mesh launches.  Every job's outputs are bit-identical to gvr_forward
+ * on the same buffers.  The plan owns all scratch (allocated at create);
+ * gvr_plan_forward allocates nothing and never synchronises the host, and
+ * gvr_plan_forward_graph captures it once into a CUDA graph and replays
+ * that graph on later calls.  The buffers named in the jobs must stay valid
+ * for the life of the plan; their contents may change between calls.
+ * Handles with compute_normal_map are refused (GVR_ERR_UNSUPPORTED). */
+typedef struct GvrPlan GvrPlan;
+
+typedef struct {
+    GvrHandle *handle;
+    GvrForwardArgs forward;  /* workspace fields ignored */
+    int32_t tile_width;      /* 8, 16 or 32 (tile height = 256 / width), or 0: chosen by the plan */
+    int32_t big_tiles;       /* 1..16: faces spanning more tiles go to the view's big-face list; 0: chosen */
+} GvrJob;
+
+/* For jobs that leave the choice to the plan: with GVR_PLAN_AUTOTUNE the
+ * plan picks, per (floor(log2 F), W, H) bucket, the fastest tile shape
+ * (16x16, 32x8, 8x32) and big-face threshold (4 or 16 tiles) by timing the
+ * first job of the bucket (the choice is cached for the process); without
+ * it they use 16x16 and 16. */
+#define GVR_PLAN_AUTOTUNE 1
+
+int gvr_plan_create(const GvrJob *jobs, int32_t count, int32_t flags, GvrPlan **out_plan);
+int gvr_plan_forward(GvrPlan *plan, void *stream);
+/* `stream` must be a created stream (graph capture cannot use the legacy default stream). */
+int gvr_plan_forward_graph(GvrPlan *plan, void *stream);
+/* The bin/tile configuration chosen for job `job`. */
+int gvr_plan_tile_config(const GvrPlan *plan, int32_t job, int32_t *tile_w, int32_t *tile_h, int32_t *big_tiles);
+void gvr_plan_destroy(GvrPlan *plan);
 
 /* Per-kernel timing, no reference counterpart.  While enabled, every kernel
  * the library launches is bracketed by a CUDA event pair on its stream;

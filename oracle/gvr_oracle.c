@@ -977,6 +977,81 @@ void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *f
     free_csr(&csr);
 }
 
+/* ------------------------------------------------------------------------- */
+/* Normal-map mode (compute_normal_map). */
+
+/* Texture-space face map (CUDABasedRasterization.cpp:241-294): each face's
+ * UV triangle in texel units (Wt*u, Ht*(1-v), 0), its box widened by 2
+ * texels, and per texel the host ray/triangle test (rayTriangleIntersectHost,
+ * :158-236, the same arithmetic as barycentric() above) of the ray from
+ * (x+.5, y+.5, 1) along -z.  Faces run in ascending order and a later face
+ * overwrites, as the reference's loop does when run serially.
+ * owner_out [Ht*Wt] = face or -1; abc_out [Ht*Wt*3] = (a, b, c) or 0. */
+void orc_uv_face_map(const float *uvs, int F, int Ht, int Wt, int32_t *owner_out, float *abc_out) {
+    for (long i = 0; i < (long)Ht * Wt; ++i) {
+        owner_out[i] = -1;
+        abc_out[3 * i] = abc_out[3 * i + 1] = abc_out[3 * i + 2] = 0.0f;
+    }
+    const f3 dir = mk3(0.0f, 0.0f, -1.0f);
+    for (int f = 0; f < F; ++f) {
+        const float *t = uvs + 6 * (size_t)f;
+        f3 t0 = mk3((float)Wt * t[0], (float)Ht * (1.0f - t[1]), 0.0f);
+        f3 t1 = mk3((float)Wt * t[2], (float)Ht * (1.0f - t[3]), 0.0f);
+        f3 t2 = mk3((float)Wt * t[4], (float)Ht * (1.0f - t[5]), 0.0f);
+        /* int(fmax(min - 2, 0)) .. int(fmin(max + 2, size)), exclusive upper bound */
+        double lx = fmax(fminf(t0.x, fminf(t1.x, t2.x)) - 2.0f, 0.0);
+        double hx = fmin(fmaxf(t0.x, fmaxf(t1.x, t2.x)) + 2.0f, (double)Wt);
+        double ly = fmax(fminf(t0.y, fminf(t1.y, t2.y)) - 2.0f, 0.0);
+        double hy = fmin(fmaxf(t0.y, fmaxf(t1.y, t2.y)) + 2.0f, (double)Ht);
+        int x0 = (int)lx, y0 = (int)ly;
+        int x1 = hx > 0.0 ? (int)hx : 0, y1 = hy > 0.0 ? (int)hy : 0;
+        for (int x = x0; x < x1; ++x)
+            for (int y = y0; y < y1; ++y) {
+                f3 abc = barycentric(mk3(x + 0.5f, y + 0.5f, 1.0f), dir, t0, t1, t2);
+                if (abc.x != -1.0f && abc.y != -1.0f && abc.z != -1.0f) {
+                    long i = (long)y * Wt + x;
+                    owner_out[i] = f;
+                    abc_out[3 * i] = abc.x; abc_out[3 * i + 1] = abc.y; abc_out[3 * i + 2] = abc.z;
+                }
+            }
+    }
+}
+
+/* renderNormalMapDevice (CUDABasedRasterization.cu:415-445) from a face map:
+ * the barycentric blend of the owner's vertex normals vn [N*3], normalised
+ * when non-zero, mapped to (n+1)/2.  Uncovered texels read face 0 with zero
+ * weights, i.e. (0.5, 0.5, 0.5).  out [Ht*Wt*3], FP32 like the reference. */
+void orc_normal_map_from(const int32_t *faces, const float *vn, const int32_t *owner, const float *abc, int Ht,
+                         int Wt, float *out) {
+    for (long i = 0; i < (long)Ht * Wt; ++i) {
+        int f = owner[i] >= 0 ? owner[i] : 0;
+        f3 w = mk3(abc[3 * i], abc[3 * i + 1], abc[3 * i + 2]);
+        f3 n0 = ld3(vn + 3 * faces[3 * f]), n1 = ld3(vn + 3 * faces[3 * f + 1]), n2 = ld3(vn + 3 * faces[3 * f + 2]);
+        f3 n = mk3(n0.x * w.x + n1.x * w.y + n2.x * w.z, n0.y * w.x + n1.y * w.y + n2.y * w.z,
+                   n0.z * w.x + n1.z * w.y + n2.z * w.z);
+        float len = sqrtf(dot3(n, n));
+        if (len != 0.0f) n = sdiv3(n, len);
+        out[3 * i] = (n.x + 1.0f) / 2.0f;
+        out[3 * i + 1] = (n.y + 1.0f) / 2.0f;
+        out[3 * i + 2] = (n.z + 1.0f) / 2.0f;
+    }
+}
+
+/* The whole normal-map forward of one batch element: vertex normals of the
+ * scene's vertices, face map at the scene's texture size, normal map. */
+void orc_normal_map(const orc_scene *s, float *out /*[Ht*Wt*3]*/) {
+    csr_t csr;
+    build_csr(s->N, s->F, s->faces, &csr);
+    float *vn = (float *)malloc((size_t)s->N * 3 * sizeof(float));
+    vertex_normals(s, &csr, vn);
+    int32_t *owner = (int32_t *)malloc((size_t)s->Ht * s->Wt * sizeof(int32_t));
+    float *abc = (float *)malloc((size_t)s->Ht * s->Wt * 3 * sizeof(float));
+    orc_uv_face_map(s->uvs, s->F, s->Ht, s->Wt, owner, abc);
+    orc_normal_map_from(s->faces, vn, owner, abc, s->Ht, s->Wt, out);
+    free(abc); free(owner); free(vn);
+    free_csr(&csr);
+}
+
 int orc_max_ties(void) { return ORC_MAX_TIES; }
 
 int orc_num_threads(void) {

@@ -55,6 +55,12 @@ def lib():
         L.orc_camera.argtypes = [P, P, P, P]
         L.orc_render_fp64.argtypes = [ctypes.POINTER(_Scene), P, P, P, P]
         L.orc_render_fp64.restype = None
+        L.orc_uv_face_map.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
+        L.orc_uv_face_map.restype = None
+        L.orc_normal_map_from.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, P]
+        L.orc_normal_map_from.restype = None
+        L.orc_normal_map.argtypes = [ctypes.POINTER(_Scene), P]
+        L.orc_normal_map.restype = None
         L.orc_max_ties.restype = ctypes.c_int
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -152,6 +158,13 @@ class OracleScene:
         lib().orc_rays(ctypes.byref(s), _ptr(out))
         return out
 
+    def normal_map(self):
+        """[Ht, Wt, 3] texture-space normal map of the normal-map mode (FP32)."""
+        out = np.empty((self.Ht, self.Wt, 3), np.float32)
+        s = self._struct()
+        lib().orc_normal_map(ctypes.byref(s), _ptr(out))
+        return out
+
     def project(self, c):
         proj = np.empty((self.N, 3), np.float32)
         bbox = np.empty((self.F, 4), np.int32)
@@ -166,6 +179,29 @@ def camera_inverse(extr12, intr9):
     invE, invP = np.empty(16, np.float32), np.empty(16, np.float32)
     lib().orc_camera(_ptr(e), _ptr(k), _ptr(invE), _ptr(invP))
     return invE.reshape(4, 4), invP.reshape(4, 4)
+
+
+def uv_face_map(uvs, Ht, Wt):
+    """(owner [Ht,Wt] int32, -1 = uncovered; abc [Ht,Wt,3]) of the normal-map
+    mode's texture-space raster (CUDABasedRasterization.cpp:241-294)."""
+    uvs = _f32(uvs).reshape(-1)
+    F = uvs.size // 6
+    owner = np.empty((Ht, Wt), np.int32)
+    abc = np.empty((Ht, Wt, 3), np.float32)
+    lib().orc_uv_face_map(_ptr(uvs), F, int(Ht), int(Wt), _ptr(owner), _ptr(abc))
+    return owner, abc
+
+
+def normal_map_from(faces, vertex_normal, owner, abc):
+    """renderNormalMapDevice (CUDABasedRasterization.cu:415-445) for a face map."""
+    faces = np.ascontiguousarray(faces, np.int32).reshape(-1)
+    vn = _f32(vertex_normal).reshape(-1)
+    owner = np.ascontiguousarray(owner, np.int32)
+    abc = _f32(abc)
+    Ht, Wt = owner.shape
+    out = np.empty((Ht, Wt, 3), np.float32)
+    lib().orc_normal_map_from(_ptr(faces), _ptr(vn), _ptr(owner), _ptr(abc), int(Ht), int(Wt), _ptr(out))
+    return out
 
 
 def num_threads() -> int:

@@ -102,8 +102,44 @@ def harness_layout():
     return out
 
 
+UVMAP_LIB = os.path.join(REF_DIR, "libref_uvmap.so")
+
+
+def build_uvmap_ref():
+    """Host library around the reference's rayTriangleIntersectHost: g++ on
+    cpp/src/Renderer/CUDABasedRasterization.cpp (unchanged, plus the same
+    clockRate shim) and refcore/uvmap_ref.cpp.  Only where the reference
+    sources are present; needs no GPU."""
+    src = os.path.join(REFERENCE, "cpp", "src")
+    if not os.path.isdir(src):
+        return False
+    os.makedirs(REF_DIR, exist_ok=True)
+    cuda = os.path.dirname(os.path.dirname(_nvcc()))
+    inc = ["-I", os.path.join(cuda, "include"), "-I",
+           os.path.join(REFERENCE, "cpp", "thirdParty", "Shared", "cutil", "inc"), "-I", os.path.join(src, "Utils"),
+           "-I", os.path.join(src, "Renderer")]
+    subprocess.run(["g++", "-O2", "-fPIC", "-fopenmp", "-w", "-shared", "-DclockRate=l2CacheSize", *inc, "-o",
+                    UVMAP_LIB, os.path.join(src, "Renderer", "CUDABasedRasterization.cpp"),
+                    os.path.join(_HERE, "refcore", "uvmap_ref.cpp"), "-L", os.path.join(cuda, "lib64"), "-lcudart"],
+                   check=True, capture_output=True)
+    return True
+
+
+def uv_face_map_reference(uvs, Ht, Wt):
+    """(owner, abc) from the reference's own host test (see build_uvmap_ref)."""
+    L = ctypes.CDLL(UVMAP_LIB)
+    P = ctypes.c_void_p
+    L.refuv_face_map.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
+    L.refuv_face_map.restype = None
+    uvs = np.ascontiguousarray(uvs, np.float32).reshape(-1)
+    owner = np.empty((Ht, Wt), np.int32)
+    abc = np.empty((Ht, Wt, 3), np.float32)
+    L.refuv_face_map(uvs.ctypes.data, uvs.size // 6, int(Ht), int(Wt), owner.ctypes.data, abc.ctypes.data)
+    return owner, abc
+
+
 def build_if_possible():
-    for step in (build_fatbins, build_harness, build_layout_lib):
+    for step in (build_fatbins, build_harness, build_layout_lib, build_uvmap_ref):
         try:
             step()
         except (subprocess.CalledProcessError, OSError):
@@ -129,6 +165,7 @@ class Refcore:
         L.refcore_forward.argtypes = [P, P, P] + [I] * 9 + [P] * 10 + [P]
         L.refcore_backward.argtypes = [P, P, P] + [I] * 11 + [P] * 16 + [P]
         L.refcore_layout.argtypes = [I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_longlong), I]
+        L.refcore_normal_map.argtypes = [P, P, I, I, I, I, P, P, P]
         self.L = L
         self._check_layout()
         h = P()
@@ -185,6 +222,26 @@ class Refcore:
             raise RuntimeError("refcore_forward: " + self.L.refcore_error().decode())
         return dict(face=face.cpu().numpy(), bary=bary.cpu().numpy(), render=img.cpu().numpy(),
                     vertex_normal=vn.cpu().numpy(), ms=ms.value)
+
+    def normal_map(self, faces, num_vertices, owner, abc, vertex_normal):
+        """renderNormalMapDevice of the reference on a face map (owner, abc)
+        and one view's vertex normals [N,3]; returns [Ht,Wt,3]."""
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        faces = np.ascontiguousarray(faces, np.int32).reshape(-1)
+        Ht, Wt = owner.shape
+        # the reference's float4 (face, a, b, c) per texel; uncovered = (0, 0, 0, 0)
+        ids = np.zeros((Ht, Wt, 4), np.float32)
+        ids[..., 0] = np.where(owner >= 0, owner, 0).astype(np.float32)
+        ids[..., 1:] = abc
+        vn = torch.from_numpy(np.ascontiguousarray(vertex_normal, np.float32)).to(dev)
+        out = torch.empty((Ht, Wt, 3), device=dev)
+        rc = self.L.refcore_normal_map(self.h, faces.ctypes.data, faces.size // 3, int(num_vertices), Ht, Wt,
+                                       ids.ctypes.data, ctypes.c_void_p(vn.data_ptr()),
+                                       ctypes.c_void_p(out.data_ptr()))
+        if rc != 0:
+            raise RuntimeError("refcore_normal_map: " + self.L.refcore_error().decode())
+        return out.cpu().numpy()
 
     def backward(self, s, fwd, b=0, albedo=None, shading=None, image_filter_size=1, with_target=False):
         """Reference gradients for the forward outputs `fwd` of the same scene."""

@@ -318,6 +318,33 @@ int refcore_backward(RefcoreHandle *h, const int32_t *faces, const float *uvs, i
     return rc;
 }
 
+// renderNormalMapDevice (CUDABasedRasterization.cu:415-445) on a texture
+// face map given as the reference's float4 (face, a, b, c) per texel (host)
+// and one view's vertex normals (device [N,3]); out is device [Ht,Wt,3].
+int refcore_normal_map(RefcoreHandle *h, const int32_t *faces, int F, int N, int Ht, int Wt,
+                       const float *texture_map_ids, const float *vnormal, float *out) {
+    if (!h) return fail("null handle");
+    DeviceBuf buf;
+    RefFwdInput in;
+    std::memset(&in, 0, sizeof(in));
+    in.numberOfCameras = 1;
+    in.F = F;
+    in.N = N;
+    in.d_facesVertex = buf.upload<int3>(faces, sizeof(int) * 3 * (size_t)F);
+    in.d_textureMapIds = buf.upload<float4>(texture_map_ids, sizeof(float4) * (size_t)Ht * Wt);
+    in.computeNormal = true;
+    in.texWidth = Wt;
+    in.texHeight = Ht;
+    in.d_vertexNormal = (float3 *)vnormal;
+    in.d_normalMap = (float3 *)out;
+    if (!in.d_facesVertex || !in.d_textureMapIds) return fail("allocation failed");
+    if (!rt_ok(cudaDeviceSynchronize(), "setup")) return -1;
+    int rc = launch(h->fwd, "renderNormalMapDevice", "CUDABasedRasterizationInput", blocks((long long)Ht * Wt), 256,
+                    &in);
+    if (!rc && !rt_ok(cudaDeviceSynchronize(), "normal map kernel")) rc = -1;
+    return rc;
+}
+
 }  // extern "C"
 #endif
 

@@ -48,3 +48,20 @@ def test_oracle_reproduces_reference_kernels(path):
             else:
                 assert rel_norm(z["ref_" + k], g[k]) < 1e-4, k
         assert rel_norm(z["ref_vertex_pos_grad"], g["vertex_pos_grad"]) < 2e-2
+
+
+UV_FIXTURES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "uvmap", "*.npz")))
+
+
+@pytest.mark.skipif(not UV_FIXTURES, reason="no face-map fixtures")
+@pytest.mark.parametrize("path", UV_FIXTURES, ids=[os.path.basename(p) for p in UV_FIXTURES])
+def test_oracle_uv_face_map_reproduces_reference(path):
+    """Normal-map mode: the oracle's texture-space face map equals the one the
+    reference's own host test produced (tests/golden/make_golden_uvmap.py),
+    owner faces and (a, b, c) bit for bit."""
+    from oracle.oracle import uv_face_map
+    z = np.load(path)
+    Ht, Wt = (int(x) for x in z["size"])
+    owner, abc = uv_face_map(z["uvs"], Ht, Wt)
+    assert np.array_equal(owner, z["owner"])
+    assert np.array_equal(abc.view(np.uint32), z["abc"].view(np.uint32))
