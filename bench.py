@@ -50,6 +50,15 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     ap.add_argument("--views", type=int, default=8, help="views of the workload (profiling runs use fewer)")
+    ap.add_argument("--workload", choices=["multiview", "batched", "fit", "learned"], default="multiview",
+                    help="multiview: the fwd+bwd step above (default); batched: 64 uneven meshes through one "
+                         "plan (forward), against the same jobs as one gvr_forward call each; fit: plain "
+                         "analysis-by-synthesis fits of the morphable model; learned: train the proposal "
+                         "network, then fit from its proposals against the plain fit")
+    ap.add_argument("--meshes", type=int, default=64, help="meshes of the batched workload")
+    ap.add_argument("--fits", type=int, default=1000, help="held-out seeds of the fit / learned workloads")
+    ap.add_argument("--train-renders", type=int, default=1_000_000, help="renders the proposal network trains on")
+    ap.add_argument("--fit-batch", type=int, default=50, help="fits run together")
     return ap.parse_args()
 
 
@@ -368,10 +377,157 @@ def run_gvr(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args):
+    """Uneven batch: `--meshes` displaced spheres with 1k..200k faces, 1..8
+    views each at 256^2/512^2/1024^2, mixed modes, 512^2 textures (views of a
+    mesh sharing a resolution form one job).  One step = the forward of every
+    job.  Timed three ways on the same buffers: the plan replayed as a CUDA
+    graph (autotuned tiles; the value), the plan launched eagerly, and one
+    gvr_forward call per job (the per-mesh loop)."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from gvr import _lib, native_build, renderer, scenes
+    from gvr.batch import BatchPlan
+    native_build.build()
+    L = _lib.load()
+    specs = scenes.uneven_batch(seed=rank, num_meshes=args.meshes)
+    jobs = []
+    for s in specs:
+        h = renderer.get_handle(s["faces"], s["uvs"], s["num_vertices"], s["num_views"], s["width"], s["height"],
+                                s["albedo_mode"], s["shading_mode"], device=dev)
+        jobs.append(dict(handle=h, vertex_pos=s["vertex_pos"], vertex_color=s["vertex_color"], texture=s["texture"],
+                         sh_coeff=s["sh_coeff"], extrinsics=s["extrinsics"], intrinsics=s["intrinsics"]))
+    t0 = time.perf_counter()
+    plan = BatchPlan(jobs, autotune=True)
+    tune_s = time.perf_counter() - t0
+    P = sum(s["num_views"] * s["width"] * s["height"] for s in specs)
+    faces = sum(s["num_views"] * s["faces"].shape[0] for s in specs)
+    stream = torch.cuda.Stream(dev)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            for _ in range(max(3, args.warmup)):
+                fn()
+            stream.synchronize()
+            barrier(world)
+            total = 0.0
+            for _ in range(args.steps):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                e1.synchronize()
+                total += e0.elapsed_time(e1)
+        return reduce_max(total / args.steps, world)
+
+    n0 = L.gvr_launch_count()
+    graph_ms = timed(lambda: plan.forward(stream=stream, graph=True))
+    eager_ms = timed(lambda: plan.forward(stream=stream))
+    n1 = L.gvr_launch_count()
+    per_call_ms = timed(lambda: plan.forward_per_call(stream=stream))
+    per_call_launches = (L.gvr_launch_count() - n1) / (max(3, args.warmup) + args.steps)
+    eager_launches = (n1 - n0) / (max(3, args.warmup) + args.steps)  # graph replays add none here
+    cfgs = {}
+    for j in range(len(jobs)):
+        cfgs.setdefault("%dx%d/%d" % plan.tile_config(j), 0)
+        cfgs["%dx%d/%d" % plan.tile_config(j)] += 1
+    if rank != 0:
+        return
+    value = world * P / (graph_ms / 1e3) / 1e6
+    line = {"metric": "batched fwd Mpix/s (64 uneven meshes)", "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": graph_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": f"uneven_batch: {args.meshes} displaced spheres, faces log-uniform 1k..200k, "
+                                   "1..8 views at 256/512/1024^2, mixed albedo x shading modes, 512^2 textures",
+                       "jobs": len(jobs), "views": sum(s["num_views"] for s in specs), "pixels": P,
+                       "view_faces": faces, "l2": "flushed between steps (256 MiB fill outside the timed events)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "faces_per_s": world * faces / (graph_ms / 1e3),
+            "plan_graph_ms": graph_ms, "plan_eager_ms": eager_ms, "per_call_ms": per_call_ms,
+            "per_call_mpix_s": P / (per_call_ms / 1e3) / 1e6,
+            "launches_per_step": {"plan": eager_launches, "per_call": per_call_launches},
+            "autotune_s": tune_s, "tile_configs": cfgs}
+    print(json.dumps(line), flush=True)
+
+
+def _fit_summary(ev, batch):
+    """Per-seed figures of a proposal.evaluate result.  A fit that never
+    reaches the goal counts with its whole run; times are per fit (the
+    batch's GPU time shared by its `batch` fits)."""
+    import numpy as np
+    steps = ev["steps_to_goal"]
+    ok = [s is not None for s in steps]
+    n = len(steps)
+    per_fit_total = ev["total_gpu_ms"] / n
+    ms = [m / batch if m is not None else None for m in ev["gpu_ms_to_goal"]]
+    solved = [m for m in ms if m is not None]
+    return {"seeds": n, "reached": int(sum(ok)), "reached_frac": sum(ok) / n,
+            "median_steps_to_goal": float(np.median([s for s in steps if s is not None])) if any(ok) else None,
+            "median_gpu_ms_to_goal_per_fit": float(np.median(solved)) if solved else None,
+            "mean_gpu_ms_to_solution_per_fit": float(np.mean([m if m is not None else per_fit_total for m in ms])),
+            "final_rmse_median": float(np.median(ev["final_rmse"])), "total_gpu_ms": ev["total_gpu_ms"]}
+
+
+def run_fit_bench(args):
+    """Analysis-by-synthesis fitting of the morphable model (28,000 vertices,
+    80 shape + 80 albedo bases, pose, 27 SH; 4 views at 512^2; 200 Adam
+    steps on photometric L2) on `--fits` held-out seeds.  `learned` first
+    trains the proposal network on `--train-renders` renders from this
+    rasteriser, then fits from its proposals (plain fit from the mean as
+    fallback when the RMSE is above 0.05 after 20 steps) and from the mean."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from gvr import fitting, native_build, proposal, tc
+    native_build.build()
+    model = fitting.MorphableModel(num_vertices=28000, seed=0, device=dev)
+    fitter = fitting.Fitter(model, num_views=4, size=512)
+    seeds = list(range(1_000_000, 1_000_000 + args.fits))
+    line = {"n_gpus": world, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic", "unit": "ms"}
+    plain = proposal.evaluate(fitter, None, seeds, batch=args.fit_batch)
+    ps = _fit_summary(plain, args.fit_batch)
+    cfg = {"workload": "morphable-model fit: 28,000 V displaced-sphere mean + 80 shape + 80 albedo smooth bases, "
+                       "pose 6, SH 27; 4 views at 512^2; 200 Adam steps on photometric L2; goal RMSE <= 0.01",
+           "fits": args.fits, "fit_batch": args.fit_batch}
+    if args.workload == "fit":
+        line.update(metric="fit GPU ms to RMSE<=0.01 (plain, per fit)", value=ps["mean_gpu_ms_to_solution_per_fit"],
+                    config=cfg, plain=ps)
+    else:
+        net = proposal.ProposalNet(dev, seed=0)
+        batch = 256
+        trainer = proposal.Trainer(model, net, batch=batch, lr=1e-3, seed=7)
+        steps = max(1, args.train_renders // batch)
+        losses, secs = trainer.train(steps, log_every=max(1, steps // 20))
+        learned = proposal.evaluate(fitter, net, seeds, batch=args.fit_batch)
+        ls = _fit_summary(learned, args.fit_batch)
+        t_l, t_p = proposal.time_to_match(learned, plain)
+        ls["mean_gpu_ms_to_plain_final_rmse_per_fit"] = float(t_l.mean())
+        ps["mean_gpu_ms_full_fit_per_fit"] = float(t_p.mean())
+        cfg.update(train_renders=steps * batch, train_batch=batch,
+                   network="5 conv 3x3/2 (3-32-64-128-256-256) + MLP 16384-512-193, BF16 tcgen05 GEMMs, FP32 accum")
+        line.update(metric="fit GPU ms to RMSE<=0.01 (learned proposal, per fit)",
+                    value=ls["mean_gpu_ms_to_solution_per_fit"], config=cfg, learned=ls, plain=ps,
+                    speedup_vs_plain=ps["mean_gpu_ms_to_solution_per_fit"] / ls["mean_gpu_ms_to_solution_per_fit"],
+                    speedup_to_plain_final_rmse=float(t_p.mean() / t_l.mean()),
+                    training={"steps": steps, "seconds": secs, "loss": losses, "tc_error": tc.tc_error()})
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload in ("fit", "learned"):
+        run_fit_bench(args)
     else:
         run_gvr(args)
     if int(os.environ.get("WORLD_SIZE", "1")) > 1:

@@ -77,11 +77,14 @@ struct BwdIO {
     int imageFilter;
 };
 
-template <int MODE, bool SHADED, bool TARGET>
+// ALBPOS (vertexColor only, opt-in): add the change of the interpolated
+// vertex colour through the barycentrics to the position gradient, which the
+// reference leaves out (CUDABasedRasterizationGrad.cu:489).
+template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
 __global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
                                                          const BwdIO io) {
     constexpr bool COL = MODE == GVR_ALBEDO_VERTEX_COLOR;
-    constexpr bool POS = SHADED || TARGET;
+    constexpr bool POS = SHADED || TARGET || ALBPOS;
     constexpr int NPOS = POS ? 9 : 0, NGN = SHADED ? 9 : 0, NCOL = COL ? 9 : 0;
     constexpr int NV = NPOS + NGN + NCOL > 0 ? NPOS + NGN + NCOL : 1;
 
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, co
             }
             // Pv: per-pixel vector applied with the stored barycentrics (target term);
             // Qv[j]: shading term already weighted for corner j
-            float Pv[3] = {0.0f, 0.0f, 0.0f}, wv[3] = {0.0f, 0.0f, 0.0f};
+            float Pv[3] = {0.0f, 0.0f, 0.0f}, wv[3] = {0.0f, 0.0f, 0.0f}, rr[3] = {0.0f, 0.0f, 0.0f};
             float Qv[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
             if (SHADED) {
                 const float ga[3] = {G[0] * alb[0], G[1] * alb[1], G[2] * alb[2]};
@@ -195,10 +198,22 @@ __global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, co
                 wv[0] = (wt[0] * len2 - un.x * wdot) * inv3;
                 wv[1] = (wt[1] * len2 - un.y * wdot) * inv3;
                 wv[2] = (wt[2] * len2 - un.z * wdot) * inv3;
-                // shading term through the barycentrics (:478-522)
-                const float r0 = wv[0] * N0.x + wv[1] * N0.y + wv[2] * N0.z;
-                const float r1 = wv[0] * N1.x + wv[1] * N1.y + wv[2] * N1.z;
-                const float r2 = wv[0] * N2.x + wv[1] * N2.y + wv[2] * N2.z;
+                // shading term through the barycentrics (:478-522): d(loss)/d(b_j) = wv . N_j
+                rr[0] = wv[0] * N0.x + wv[1] * N0.y + wv[2] * N0.z;
+                rr[1] = wv[0] * N1.x + wv[1] * N1.y + wv[2] * N1.z;
+                rr[2] = wv[0] * N2.x + wv[1] * N2.y + wv[2] * N2.z;
+            }
+            if (ALBPOS) {  // + sum_ch G light colour_j
+                const float *Cb = io.colors + (size_t)b * N * 3;
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                    const float lg = G[ch] * JCoAl[ch];
+                    rr[0] += lg * Cb[3 * i0 + ch];
+                    rr[1] += lg * Cb[3 * i1 + ch];
+                    rr[2] += lg * Cb[3 * i2 + ch];
+                }
+            }
+            if (SHADED || ALBPOS) {
                 const float *Vb = io.verts + (size_t)b * N * 3;
                 const float3 V0 = make_float3(Vb[3 * i0], Vb[3 * i0 + 1], Vb[3 * i0 + 2]);
                 const float3 e1 = make_float3(Vb[3 * i1] - V0.x, Vb[3 * i1 + 1] - V0.y, Vb[3 * i1 + 2] - V0.z);
@@ -235,7 +250,7 @@ __global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, co
                                                   (e2.x * d.y - e2.y * d.x) * inv);
                     const float3 g2 = make_float3((d.y * e1.z - d.z * e1.y) * inv, (d.z * e1.x - d.x * e1.z) * inv,
                                                   (d.x * e1.y - d.y * e1.x) * inv);
-                    const float k1 = r1 - r0, k2 = r2 - r0;
+                    const float k1 = rr[1] - rr[0], k2 = rr[2] - rr[0];
                     const float q[3] = {k1 * g1.x + k2 * g2.x, k1 * g1.y + k2 * g2.y, k1 * g1.z + k2 * g2.z};
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
@@ -434,21 +449,30 @@ __global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ p
 
 static inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
 
-template <int MODE, bool SHADED, bool TARGET>
+template <int MODE, bool SHADED, bool TARGET, bool ALBPOS>
 static cudaError_t launch_pixels_t(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const BwdIO &io,
                                    cudaStream_t st) {
     const int grid = dims.B * dims.C * dims.tilesX * dims.tilesY;
-    GVR_LAUNCH(st, "k_bwd_pixels", (k_bwd_pixels<MODE, SHADED, TARGET><<<grid, kTilePix, 0, st>>>(topo, dims, ws, io)));
+    GVR_LAUNCH(st, "k_bwd_pixels",
+               (k_bwd_pixels<MODE, SHADED, TARGET, ALBPOS><<<grid, kTilePix, 0, st>>>(topo, dims, ws, io)));
     return cudaGetLastError();
 }
 
-template <int MODE>
-static cudaError_t launch_pixels_m(bool shaded, bool target, const Topology &topo, const FrameDims &dims,
+template <int MODE, bool ALBPOS>
+static cudaError_t launch_pixels_a(bool shaded, bool target, const Topology &topo, const FrameDims &dims,
                                    const BwdScratch &ws, const BwdIO &io, cudaStream_t st) {
-    if (shaded) return target ? launch_pixels_t<MODE, true, true>(topo, dims, ws, io, st)
-                              : launch_pixels_t<MODE, true, false>(topo, dims, ws, io, st);
-    return target ? launch_pixels_t<MODE, false, true>(topo, dims, ws, io, st)
-                  : launch_pixels_t<MODE, false, false>(topo, dims, ws, io, st);
+    if (shaded) return target ? launch_pixels_t<MODE, true, true, ALBPOS>(topo, dims, ws, io, st)
+                              : launch_pixels_t<MODE, true, false, ALBPOS>(topo, dims, ws, io, st);
+    return target ? launch_pixels_t<MODE, false, true, ALBPOS>(topo, dims, ws, io, st)
+                  : launch_pixels_t<MODE, false, false, ALBPOS>(topo, dims, ws, io, st);
+}
+
+template <int MODE>
+static cudaError_t launch_pixels_m(bool shaded, bool target, bool albpos, const Topology &topo, const FrameDims &dims,
+                                   const BwdScratch &ws, const BwdIO &io, cudaStream_t st) {
+    if constexpr (MODE == GVR_ALBEDO_VERTEX_COLOR)
+        if (albpos) return launch_pixels_a<MODE, true>(shaded, target, topo, dims, ws, io, st);
+    return launch_pixels_a<MODE, false>(shaded, target, topo, dims, ws, io, st);
 }
 
 cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const GvrBackwardArgs &a,
@@ -471,10 +495,15 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     if ((err = launch_face_geo(a.vertex_pos, topo, ws.geo, nullptr, B, st))) return err;
     BwdIO io{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image, a.vertex_normal,
              a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter};
+    const bool albpos = (a.flags & GVR_BACKWARD_ALBEDO_POSITION) != 0;
     switch (dims.albedo) {
-        case GVR_ALBEDO_VERTEX_COLOR: err = launch_pixels_m<GVR_ALBEDO_VERTEX_COLOR>(shaded, target, topo, dims, ws, io, st); break;
-        case GVR_ALBEDO_TEXTURED: err = launch_pixels_m<GVR_ALBEDO_TEXTURED>(shaded, target, topo, dims, ws, io, st); break;
-        default: err = launch_pixels_m<GVR_ALBEDO_FOREGROUND_MASK>(false, target, topo, dims, ws, io, st); break;
+        case GVR_ALBEDO_VERTEX_COLOR:
+            err = launch_pixels_m<GVR_ALBEDO_VERTEX_COLOR>(shaded, target, albpos, topo, dims, ws, io, st);
+            break;
+        case GVR_ALBEDO_TEXTURED:
+            err = launch_pixels_m<GVR_ALBEDO_TEXTURED>(shaded, target, false, topo, dims, ws, io, st);
+            break;
+        default: err = launch_pixels_m<GVR_ALBEDO_FOREGROUND_MASK>(false, target, false, topo, dims, ws, io, st); break;
     }
     if (err) return err;
     GVR_LAUNCH(st, "k_gather_a",

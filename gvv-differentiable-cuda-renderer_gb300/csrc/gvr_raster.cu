@@ -152,16 +152,43 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     const int s0 = ws.tileStart[tIdx], nTile = ws.tileStart[tIdx + 1] - s0;
     const int nAll = nTile + ws.bigCount[bc];
 
-    // stage the entries whose triangle may cover a pixel of the tile (compacted in any order)
-    __shared__ float sKey[kCachedEntries];
-    if (tid == 0) sCount = 0;
-    __syncthreads();
     const int lane = tid & 31;
-    for (int e0 = 0; e0 < nAll; e0 += kTilePix) {
+    // the pixel rows of this warp (32 / tileW rows of tileW pixels)
+    const int rowLo = tileY0 + ((tid & ~31) >> dims.tileShift), rowHi = rowLo + (32 >> dims.tileShift) - 1;
+    const float kInf = __int_as_float(0x7f800000);
+    __shared__ float sKey[kCachedEntries];
+    __shared__ short sOrder[kCachedEntries];
+    __shared__ float sBucketLo[kCachedEntries];
+    __shared__ int sHist[kBuckets + 1];
+    __shared__ unsigned sKeyLo, sKeyHi;
+
+    // One pass front to back: `zup` is the smallest certain depth bound so
+    // far; candidates (face, lower depth bound) are kept while their bound
+    // does not exceed it.  A bound only decreases, so a face dropped early
+    // could never win; the survivors are filtered again by the final bound.
+    // The tile's entries go through shared memory in chunks of
+    // kCachedEntries (dense meshes at low resolution put thousands of faces
+    // in a tile); zup and the candidates carry over from chunk to chunk.
+    float zup = kInf;
+    int nCand = 0;
+    bool spill = false;
+    int cf[kMaxCand];
+    float cz[kMaxCand];
+#pragma unroll
+    for (int j = 0; j < kMaxCand; ++j) {
+        cf[j] = -1;
+        cz[j] = kInf;
+    }
+    for (int c0 = 0; c0 < nAll; c0 += kCachedEntries) {
+    const int cEnd = min(nAll, c0 + kCachedEntries);
+    // stage the chunk's entries whose triangle may cover a pixel of the tile (compacted in any order)
+    if (tid == 0) sCount = 0;
+    __syncthreads();  // (also: every warp is done walking the previous chunk)
+    for (int e0 = c0; e0 < cEnd; e0 += kTilePix) {
         const int e = e0 + tid;
         bool keep = false;
         Entry E;
-        if (e < nAll) {
+        if (e < cEnd) {
             const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
             E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
             keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
@@ -171,28 +198,19 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         if (lane == 0 && m) base = atomicAdd(&sCount, __popc(m));
         base = __shfl_sync(0xffffffffu, base, 0);
         if (keep) {
-            const int slot = base + __popc(m & ((1u << lane) - 1u));
-            if (slot < kCachedEntries) {
-                sE[slot] = E;
-                sKey[slot] = E.zLowSafe;
-            }
+            const int slot = base + __popc(m & ((1u << lane) - 1u));  // < cEnd - c0 <= kCachedEntries
+            sE[slot] = E;
+            sKey[slot] = E.zLowSafe;
         }
     }
     __syncthreads();
     const int nE = sCount;
-    const bool overflow = nE > kCachedEntries;  // block-uniform: then walk the global list instead
-    // the pixel rows of this warp (32 / tileW rows of tileW pixels)
-    const int rowLo = tileY0 + ((tid & ~31) >> dims.tileShift), rowHi = rowLo + (32 >> dims.tileShift) - 1;
 
     // Front-to-back order: counting sort into kBuckets depth buckets spanning
-    // the tile's finite depth lower bounds (faces without a bound go first).
+    // the chunk's finite depth lower bounds (faces without a bound go first).
     // sBucketLo[i] is a lower bound of the depth bound of entry i and of
     // every entry after it, which is all the early exit needs.
-    __shared__ short sOrder[kCachedEntries];
-    __shared__ float sBucketLo[kCachedEntries];
-    __shared__ int sHist[kBuckets + 1];
-    __shared__ unsigned sKeyLo, sKeyHi;
-    if (!overflow) {
+    {
         if (tid == 0) {
             sKeyLo = 0x7f800000u;
             sKeyHi = 0u;
@@ -217,9 +235,9 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         __syncthreads();
         if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: 3 per lane, one warp scan
             const int q0 = 3 * tid;
-            const int c0 = q0 <= kBuckets ? sHist[q0] : 0, c1 = q0 + 1 <= kBuckets ? sHist[q0 + 1] : 0,
-                      c2 = q0 + 2 <= kBuckets ? sHist[q0 + 2] : 0;
-            const int own = c0 + c1 + c2;
+            const int h0 = q0 <= kBuckets ? sHist[q0] : 0, h1 = q0 + 1 <= kBuckets ? sHist[q0 + 1] : 0,
+                      h2 = q0 + 2 <= kBuckets ? sHist[q0 + 2] : 0;
+            const int own = h0 + h1 + h2;
             int incl = own;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -228,8 +246,8 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             }
             const int ex = incl - own;
             if (q0 <= kBuckets) sHist[q0] = ex;
-            if (q0 + 1 <= kBuckets) sHist[q0 + 1] = ex + c0;
-            if (q0 + 2 <= kBuckets) sHist[q0 + 2] = ex + c0 + c1;
+            if (q0 + 1 <= kBuckets) sHist[q0 + 1] = ex + h0;
+            if (q0 + 2 <= kBuckets) sHist[q0 + 2] = ex + h0 + h1;
         }
         __syncthreads();
         for (int e = tid; e < nE; e += kTilePix) {
@@ -243,37 +261,10 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     }
     __syncthreads();
 
-    auto entry_at = [&](int i, Entry &E) -> bool {
-        if (!overflow) {
-            E = sE[sOrder[i]];
-            return true;
-        }
-        const int f = i < nTile ? ws.bins[s0 + i] : bigList[i - nTile];
-        E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
-        return E.bx0 <= E.bx1 && E.by0 <= E.by1;
-    };
-    const int nWalk = overflow ? nAll : nE;
-    const float kInf = __int_as_float(0x7f800000);
-
-    // One pass front to back: `zup` is the smallest certain depth bound so
-    // far; candidates (face, lower depth bound) are kept while their bound
-    // does not exceed it.  A bound only decreases, so a face dropped early
-    // could never win; the survivors are filtered again by the final bound.
-    float zup = kInf;
-    int nCand = 0;
-    bool spill = false;
-    int cf[kMaxCand];
-    float cz[kMaxCand];
-#pragma unroll
-    for (int j = 0; j < kMaxCand; ++j) {
-        cf[j] = -1;
-        cz[j] = kInf;
-    }
-    for (int i = 0; i < nWalk; ++i) {
-        Entry E;
-        if (!entry_at(i, E)) continue;
-        // every later entry lies behind every pixel of this warp: stop (sorted order only)
-        if (!overflow && sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
+    for (int i = 0; i < nE; ++i) {
+        const Entry E = sE[sOrder[i]];
+        // every later entry of the chunk lies behind every pixel of this warp: stop
+        if (sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
         if (E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
         if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
         if (E.zLowSafe > zup) continue;  // behind this pixel's covering face (and so is every later entry)
@@ -316,6 +307,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             }
         ++nCand;
     }
+    }  // chunks
 
     if (u >= dims.W || v >= dims.H) return;
 
@@ -343,9 +335,9 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             }
         }
     } else {  // more candidates than registers: test every face that may win against the final bound
-        for (int e = 0; e < nWalk; ++e) {
-            Entry E;
-            if (!entry_at(e, E)) continue;
+        for (int e = 0; e < nAll; ++e) {
+            const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
+            const Entry E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
             if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
             if (!may_win(E, px, py, zup)) continue;
             V3 t;
@@ -424,7 +416,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
 }  // namespace
 
 // One block per tile of one call.
-__global__ void __launch_bounds__(kTilePix) k_raster(const FwdJob J) { raster_tile(J, blockIdx.x); }
+__global__ void __launch_bounds__(kTilePix, 4) k_raster(const FwdJob J) { raster_tile(J, blockIdx.x); }
 
 // Persistent: a grid sized to the resident capacity pulls (job, view, tile)
 // items from one counter until all jobs' tiles are done.  itemStart[j] is the

@@ -41,7 +41,10 @@ class GvrBackwardArgs(ctypes.Structure):
                 ("target_image", P), ("vertex_normal", P), ("barycentric", P), ("face", P), ("target_grad", P),
                 ("extrinsics", P), ("intrinsics", P),
                 ("vertex_pos_grad", P), ("vertex_color_grad", P), ("texture_grad", P), ("sh_coeff_grad", P),
-                ("workspace", P), ("workspace_bytes", ctypes.c_size_t)]
+                ("workspace", P), ("workspace_bytes", ctypes.c_size_t), ("flags", I32)]
+
+
+BACKWARD_ALBEDO_POSITION = 1  # GVR_BACKWARD_ALBEDO_POSITION
 
 
 class GvrJob(ctypes.Structure):
@@ -60,7 +63,9 @@ EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forw
            "gvr_backward_workspace_size", "gvr_last_error", "gvr_abi_version", "gvr_debug_rays",
            "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc",
            "gvr_plan_create", "gvr_plan_forward", "gvr_plan_forward_graph", "gvr_plan_tile_config",
-           "gvr_plan_destroy")
+           "gvr_plan_destroy",
+           # include/gvr_nn.h
+           "gvr_gemm_bf16", "gvr_tc_error", "gvr_im2col_3x3s2", "gvr_col2im_3x3s2", "gvr_nn_last_error")
 
 NOALLOC_SCRATCH_BYTES = 32 << 20  # GVR_NOALLOC_SCRATCH_BYTES
 

@@ -79,6 +79,25 @@ class BatchPlan:
         _lib.check(fn(self._plan, s))
         return self.outputs
 
+    def forward_per_call(self, stream=None):
+        """The same jobs through gvr_forward one by one (one launch chain per
+        job, default tiles) into the same outputs: the per-mesh loop the
+        plan replaces."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        s = ctypes.c_void_p(st.cuda_stream)
+        if not hasattr(self, "_ws"):
+            need = max(int(self._L.gvr_forward_workspace_size(self.handles[j].ptr, self._jobs[j].forward.batch,
+                                                              self._jobs[j].forward.texture_height,
+                                                              self._jobs[j].forward.texture_width))
+                       for j in range(len(self.handles)))
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        for j, h in enumerate(self.handles):
+            args = _lib.GvrForwardArgs.from_buffer_copy(self._jobs[j].forward)
+            args.workspace = ctypes.c_void_p(self._ws.data_ptr())
+            args.workspace_bytes = self._ws.numel()
+            _lib.check(self._L.gvr_forward(h.ptr, ctypes.byref(args), s))
+        return self.outputs
+
     def tile_config(self, j):
         w, h, b = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         _lib.check(self._L.gvr_plan_tile_config(self._plan, j, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b)))

@@ -168,8 +168,9 @@ def render_forward(h: RendererHandle, vertex_pos, vertex_color, texture, sh_coef
 
 
 def render_backward(h: RendererHandle, grad_render, vertex_pos, vertex_color, texture, sh_coeff, target_image,
-                    vertex_normal, barycentric, face, grad_target, extrinsics, intrinsics):
-    """Gradients (vertex_pos, vertex_color, texture, sh_coeff) of CudaRendererGradGpu."""
+                    vertex_normal, barycentric, face, grad_target, extrinsics, intrinsics, flags=0):
+    """Gradients (vertex_pos, vertex_color, texture, sh_coeff) of CudaRendererGradGpu.
+    flags: GVR_BACKWARD_* options (_lib.BACKWARD_ALBEDO_POSITION); 0 = the reference's gradient."""
     dev = h.device
     B = vertex_pos.shape[0]
     Ht, Wt = texture.shape[1], texture.shape[2]
@@ -189,7 +190,7 @@ def render_backward(h: RendererHandle, grad_render, vertex_pos, vertex_color, te
     args = _lib.GvrBackwardArgs(B, Ht, Wt, _ptr(grad_render), _ptr(vertex_pos), _ptr(vertex_color), _ptr(texture),
                                 _ptr(sh_coeff), _ptr(target_image), _ptr(vertex_normal), _ptr(barycentric),
                                 _ptr(face), _ptr(grad_target), _ptr(extrinsics), _ptr(intrinsics),
-                                _ptr(gp), _ptr(gc), _ptr(gt), _ptr(gs), _ptr(ws), ws_bytes)
+                                _ptr(gp), _ptr(gc), _ptr(gt), _ptr(gs), _ptr(ws), ws_bytes, int(flags))
     _lib.check(h._L.gvr_backward(h.ptr, ctypes.byref(args), _stream(dev)))
     return gp, gc, gt, gs
 
@@ -201,10 +202,12 @@ class RenderFunction(torch.autograd.Function):
     extrinsics and intrinsics get none (python/CudaRenderer.py:215)."""
 
     @staticmethod
-    def forward(ctx, h, vertex_pos, vertex_color, texture, sh_coeff, target_image, extrinsics, intrinsics):
+    def forward(ctx, h, vertex_pos, vertex_color, texture, sh_coeff, target_image, extrinsics, intrinsics,
+                backward_flags=0):
         bary, face, img, vnorm, tout, nmap = render_forward(h, vertex_pos, vertex_color, texture, sh_coeff,
                                                             extrinsics, intrinsics, target_image, copy_target=True)
         ctx.h = h
+        ctx.backward_flags = backward_flags
         ctx.save_for_backward(vertex_pos, vertex_color, texture, sh_coeff, target_image, extrinsics, intrinsics,
                               face, vnorm)
         ctx.mark_non_differentiable(face, bary, vnorm, nmap)
@@ -214,8 +217,9 @@ class RenderFunction(torch.autograd.Function):
     def backward(ctx, g_bary, g_face, g_render, g_vnorm, g_target, g_nmap):
         vp, vc, tex, sh, tgt, ex, ix, face, vnorm = ctx.saved_tensors
         h = ctx.h
-        gp, gc, gt, gs = render_backward(h, g_render, vp, vc, tex, sh, tgt, vnorm, None, face, g_target, ex, ix)
-        return None, gp, gc, gt, gs, None, None, None
+        gp, gc, gt, gs = render_backward(h, g_render, vp, vc, tex, sh, tgt, vnorm, None, face, g_target, ex, ix,
+                                         ctx.backward_flags)
+        return None, gp, gc, gt, gs, None, None, None, None
 
 
 class CudaRendererGpu:

@@ -125,7 +125,16 @@ typedef struct {
     float *sh_coeff_grad;         /* out [B,C,27]                               */
     void *workspace;
     size_t workspace_bytes;
+    int32_t flags;                /* 0 = the reference's gradient; GVR_BACKWARD_* options */
 } GvrBackwardArgs;
+
+/* Backward option without reference counterpart (vertexColor mode only):
+ * also propagate the change of the interpolated vertex colour through the
+ * barycentrics into vertex_pos_grad.  The reference leaves this term out
+ * (CUDABasedRasterizationGrad.cu:489), so its position gradient is the
+ * loss's derivative only for constant colours; fitting with per-vertex
+ * colours needs the term.  Ignored in the other modes. */
+#define GVR_BACKWARD_ALBEDO_POSITION 1
 
 /* Builds the device topology and vertex->face adjacency in O(F)
  * (replaces the O(N*F) getVertexFaces, CUDABasedRasterization.cpp:125-154).

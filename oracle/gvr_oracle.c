@@ -299,6 +299,18 @@ static void vertex_normals(const orc_scene *s, const csr_t *csr, float *vn /*[N*
 /* Shading helpers */
 
 /* getShading / getIllum (RendererUtil.h:135-214), FP64. */
+static d3 sh_light_d(d3 n, const double *sh) {
+    double basis[9] = {1.0, n.y, n.z, n.x, n.x * n.y, n.z * n.y, 3.0 * n.z * n.z - 1.0, n.x * n.z,
+                       n.x * n.x - n.y * n.y};
+    double l[3];
+    for (int ch = 0; ch < 3; ++ch) {
+        double acc = 0.0;
+        for (int k = 0; k < 9; ++k) acc += sh[9 * ch + k] * basis[k];
+        l[ch] = acc;
+    }
+    return dk3(l[0], l[1], l[2]);
+}
+
 static d3 sh_light(d3 n, const float *sh) {
     double basis[9] = {1.0, n.y, n.z, n.x, n.x * n.y, n.z * n.y, 3.0 * n.z * n.z - 1.0, n.x * n.z,
                        n.x * n.x - n.y * n.y};
@@ -682,9 +694,13 @@ static void J_projection(d3 X, const float *intr9, const float *extr12, double J
  * FP64 and fully overwritten:
  *   gpos [N*3], gcol [N*3], gtex [Ht*Wt*3], gsh [C*27].
  */
-void orc_backward(const orc_scene *s, const int32_t *face, const float *bary, const float *vnormal,
-                  const float *grad_render, const float *target, const float *grad_target, double *gpos,
-                  double *gcol, double *gtex, double *gsh) {
+/* flags & 1 (GVR_BACKWARD_ALBEDO_POSITION, an option without reference
+ * counterpart): vertexColor mode also moves the vertices by the change of
+ * the interpolated colour through the barycentrics, the term the reference
+ * zeroes (CUDABasedRasterizationGrad.cu:489). */
+void orc_backward_ex(const orc_scene *s, const int32_t *face, const float *bary, const float *vnormal,
+                     const float *grad_render, const float *target, const float *grad_target, double *gpos,
+                     double *gcol, double *gtex, double *gsh, int flags) {
     const int N = s->N, W = s->W, H = s->H, C = s->C;
     csr_t csr;
     build_csr(N, s->F, s->faces, &csr);
@@ -795,12 +811,16 @@ void orc_backward(const orc_scene *s, const int32_t *face, const float *bary, co
                     }
                     /* vertex position, shading term (:458-525) */
                     d3 w = dk3(0, 0, 0);
-                    if (shaded) {
-                        m33 JLiNo = J_light_normal(n, sh);
-                        m33 JNoNu = J_normalize(un, unLen);
-                        w = rowmul(rowmul(rowmul(G, JCoLi), JLiNo), JNoNu);
-                        m33 JNoBc = m33_cols(Nor[0], Nor[1], Nor[2]);
-                        d3 r = rowmul(w, JNoBc);
+                    const int albpos = (flags & 1) && s->albedo_mode == ORC_VERTEX_COLOR;
+                    if (shaded || albpos) {
+                        d3 r = dk3(0, 0, 0);
+                        if (shaded) {
+                            m33 JLiNo = J_light_normal(n, sh);
+                            m33 JNoNu = J_normalize(un, unLen);
+                            w = rowmul(rowmul(rowmul(G, JCoLi), JLiNo), JNoNu);
+                            r = rowmul(w, m33_cols(Nor[0], Nor[1], Nor[2]));
+                        }
+                        if (albpos) r = dadd(r, rowmul(rowmul(G, JCoAl), m33_cols(Col[0], Col[1], Col[2])));
                         double JB[3][9];
                         J_bary_pos(o, d, P[0], P[1], P[2], JB);
                         for (int var = 0; var < 9; ++var) {
@@ -854,6 +874,12 @@ void orc_backward(const orc_scene *s, const int32_t *face, const float *bary, co
     free_csr(&csr);
 }
 
+void orc_backward(const orc_scene *s, const int32_t *face, const float *bary, const float *vnormal,
+                  const float *grad_render, const float *target, const float *grad_target, double *gpos,
+                  double *gcol, double *gtex, double *gsh) {
+    orc_backward_ex(s, face, bary, vnormal, grad_render, target, grad_target, gpos, gcol, gtex, gsh, 0);
+}
+
 /* ------------------------------------------------------------------------- */
 /* FP64 forward at fixed visibility, for finite-difference checks of the
  * gradient restatement: given face ids per pixel, every quantity (camera
@@ -862,6 +888,7 @@ void orc_backward(const orc_scene *s, const int32_t *face, const float *bary, co
  * flags_out bit 0: normal flipped; bit 1: |cos(ray, face normal)| < 0.002
  * (near the reference Jacobian's 0.001 early-out). */
 #define VD(i) (verts_d ? dk3(verts_d[3 * (i)], verts_d[3 * (i) + 1], verts_d[3 * (i) + 2]) : ldd3(s->verts + 3 * (i)))
+#define CD(i) (colors_d ? dk3(colors_d[3 * (i)], colors_d[3 * (i) + 1], colors_d[3 * (i) + 2]) : ldd3(s->colors + 3 * (i)))
 
 static void mat4_inverse_d(const double *m, double *inv) {
     double a[4][8];
@@ -884,8 +911,11 @@ static void mat4_inverse_d(const double *m, double *inv) {
         for (int j = 0; j < 4; ++j) inv[4 * i + j] = a[i][4 + j];
 }
 
-void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *face, double *render_out,
-                     int32_t *flags_out) {
+/* FP64 render at fixed visibility; verts_d [N*3], colors_d [N*3] and sh_d
+ * [C*27] optionally replace the scene's FP32 arrays (finite differences of
+ * parameters that feed them). */
+void orc_render_fp64_ex(const orc_scene *s, const double *verts_d, const double *colors_d, const double *sh_d,
+                        const int32_t *face, double *render_out, int32_t *flags_out) {
     const int N = s->N, F = s->F, W = s->W, H = s->H;
     csr_t csr;
     build_csr(N, F, s->faces, &csr);
@@ -902,7 +932,9 @@ void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *f
         vn[v] = acc;
     }
     for (int c = 0; c < s->C; ++c) {
-        const float *e12 = s->extr + 12 * c, *k9 = s->intr + 9 * c, *sh = s->sh + 27 * c;
+        const float *e12 = s->extr + 12 * c, *k9 = s->intr + 9 * c;
+        double sh[27];
+        for (int k = 0; k < 27; ++k) sh[k] = sh_d ? sh_d[27 * c + k] : (double)s->sh[27 * c + k];
         double E[16] = {0}, K[16] = {0}, KE[16], invE[16], invP[16];
         for (int i = 0; i < 16; ++i) E[i] = K[i] = (i % 5 == 0);
         for (int r = 0; r < 3; ++r)
@@ -943,8 +975,10 @@ void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *f
                 int flip = ddot(n, d) > 0.0;
                 if (flip) n = dscale(-1.0, n);
                 if (flags_out) {
+                    /* 1: normal flipped; 2: grazing face (|cos| < 0.002); 4: interpolated normal within
+                     * 0.01 of perpendicular to the ray, where a small change of the inputs can flip it */
                     double cosv = fabs(ddot(d, Nf)) / sqrt(den);
-                    flags_out[p] = flip | ((cosv < 0.002) << 1);
+                    flags_out[p] = flip | ((cosv < 0.002) << 1) | ((fabs(ddot(n, d)) < 0.01) << 2);
                 }
                 d3 col;
                 if (s->albedo_mode == ORC_TEXTURED) {
@@ -956,8 +990,7 @@ void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *f
                     int LU = (int)(U - 0.5), LV = (int)(V - 0.5);
                     col = ldd3(s->texture + ((size_t)LV * s->Wt + LU) * 3);
                 } else if (s->albedo_mode == ORC_VERTEX_COLOR) {
-                    col = dadd(dadd(dscale(a, ldd3(s->colors + 3 * i0)), dscale(b, ldd3(s->colors + 3 * i1))),
-                               dscale(cc, ldd3(s->colors + 3 * i2)));
+                    col = dadd(dadd(dscale(a, CD(i0)), dscale(b, CD(i1))), dscale(cc, CD(i2)));
                 } else if (s->albedo_mode == ORC_NORMAL) {
                     col = dk3((1.0 + n.x) / 2.0, (1.0 + n.y) / 2.0, (1.0 + n.z) / 2.0);
                 } else {
@@ -967,7 +1000,7 @@ void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *f
                              s->albedo_mode == ORC_LIGHTING;
                 if (s->albedo_mode == ORC_FOREGROUND) shaded = 0;
                 if (shaded) {
-                    d3 l = sh_light(n, sh);
+                    d3 l = sh_light_d(n, sh);
                     col = dk3(l.x * col.x, l.y * col.y, l.z * col.z);
                 }
                 out[0] = col.x; out[1] = col.y; out[2] = col.z;
@@ -1050,6 +1083,11 @@ void orc_normal_map(const orc_scene *s, float *out /*[Ht*Wt*3]*/) {
     orc_normal_map_from(s->faces, vn, owner, abc, s->Ht, s->Wt, out);
     free(abc); free(owner); free(vn);
     free_csr(&csr);
+}
+
+void orc_render_fp64(const orc_scene *s, const double *verts_d, const int32_t *face, double *render_out,
+                     int32_t *flags_out) {
+    orc_render_fp64_ex(s, verts_d, NULL, NULL, face, render_out, flags_out);
 }
 
 int orc_max_ties(void) { return ORC_MAX_TIES; }

@@ -50,11 +50,15 @@ def lib():
         L.orc_forward.restype = None
         L.orc_backward.argtypes = [ctypes.POINTER(_Scene), P, P, P, P, P, P, P, P, P, P]
         L.orc_backward.restype = None
+        L.orc_backward_ex.argtypes = [ctypes.POINTER(_Scene), P, P, P, P, P, P, P, P, P, P, ctypes.c_int]
+        L.orc_backward_ex.restype = None
         L.orc_rays.argtypes = [ctypes.POINTER(_Scene), P]
         L.orc_project.argtypes = [ctypes.POINTER(_Scene), ctypes.c_int, P, P]
         L.orc_camera.argtypes = [P, P, P, P]
         L.orc_render_fp64.argtypes = [ctypes.POINTER(_Scene), P, P, P, P]
         L.orc_render_fp64.restype = None
+        L.orc_render_fp64_ex.argtypes = [ctypes.POINTER(_Scene), P, P, P, P, P, P]
+        L.orc_render_fp64_ex.restype = None
         L.orc_uv_face_map.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
         L.orc_uv_face_map.restype = None
         L.orc_normal_map_from.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, P]
@@ -120,7 +124,9 @@ class OracleScene:
                           _ptr(out["tie_faces"]))
         return out
 
-    def backward(self, face, bary, vertex_normal, grad_render, target, grad_target):
+    def backward(self, face, bary, vertex_normal, grad_render, target, grad_target, flags=0):
+        """flags & 1: also the vertex colour's change through the barycentrics
+        (the GVR_BACKWARD_ALBEDO_POSITION option)."""
         N, C = self.N, self.C
         face = np.ascontiguousarray(face, np.int32)
         bary, vertex_normal = _f32(bary), _f32(vertex_normal)
@@ -128,20 +134,26 @@ class OracleScene:
         out = dict(vertex_pos_grad=np.empty((N, 3)), vertex_color_grad=np.empty((N, 3)),
                    texture_grad=np.empty((self.Ht, self.Wt, 3)), sh_coeff_grad=np.empty((C, 27)))
         s = self._struct()
-        lib().orc_backward(ctypes.byref(s), _ptr(face), _ptr(bary), _ptr(vertex_normal), _ptr(grad_render),
-                           _ptr(target), _ptr(grad_target), _ptr(out["vertex_pos_grad"]),
-                           _ptr(out["vertex_color_grad"]), _ptr(out["texture_grad"]), _ptr(out["sh_coeff_grad"]))
+        lib().orc_backward_ex(ctypes.byref(s), _ptr(face), _ptr(bary), _ptr(vertex_normal), _ptr(grad_render),
+                              _ptr(target), _ptr(grad_target), _ptr(out["vertex_pos_grad"]),
+                              _ptr(out["vertex_color_grad"]), _ptr(out["texture_grad"]), _ptr(out["sh_coeff_grad"]),
+                              int(flags))
         return out
 
-    def render_fp64(self, face, verts_d=None):
+    def render_fp64(self, face, verts_d=None, colors_d=None, sh_d=None):
         """FP64 render at fixed visibility `face` [C,H,W]; returns (render, flags).
-        `verts_d` optionally gives FP64 vertex positions [N,3]."""
+        `verts_d` [N,3], `colors_d` [N,3] and `sh_d` [C,27] optionally give
+        FP64 values in place of the scene's FP32 arrays.  flags per pixel:
+        1 normal flipped toward the camera, 2 grazing face, 4 interpolated
+        normal within 0.01 of perpendicular to the ray (a small input change
+        can flip it) -- pixels where finite differences are not meaningful."""
         face = np.ascontiguousarray(face, np.int32)
-        vd = None if verts_d is None else np.ascontiguousarray(verts_d, np.float64).reshape(-1)
+        dbl = lambda a: None if a is None else np.ascontiguousarray(a, np.float64).reshape(-1)
+        vd, cd, sd = dbl(verts_d), dbl(colors_d), dbl(sh_d)
         out = np.empty((self.C, self.H, self.W, 3), np.float64)
         flags = np.empty((self.C, self.H, self.W), np.int32)
         s = self._struct()
-        lib().orc_render_fp64(ctypes.byref(s), _ptr(vd), _ptr(face), _ptr(out), _ptr(flags))
+        lib().orc_render_fp64_ex(ctypes.byref(s), _ptr(vd), _ptr(cd), _ptr(sd), _ptr(face), _ptr(out), _ptr(flags))
         return out, flags
 
     def with_(self, **kw):

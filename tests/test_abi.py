@@ -1,7 +1,8 @@
 """C-ABI checks that need no GPU: libgvr.so builds, loads, exports every
-symbol include/gvr.h declares, and rejects bad arguments with a status code
-(validation runs on the host before any CUDA call)."""
+symbol the headers in include/ declare, and rejects bad arguments with a
+status code (validation runs on the host before any CUDA call)."""
 import ctypes
+import glob
 import os
 import re
 
@@ -11,10 +12,11 @@ import pytest
 from conftest import REPO
 
 HEADER = os.path.join(REPO, "include", "gvr.h")
+HEADERS = sorted(glob.glob(os.path.join(REPO, "include", "*.h")))
 
 
 def _declared():
-    src = open(HEADER).read()
+    src = "\n".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"^\s*(?:int|void|size_t|long long|const char \*)\s*\*?\s*(gvr_\w+)\s*\(", src, re.M)))
 
 

@@ -41,7 +41,7 @@ def _handle(s, albedo=None, shading=None, image_filter_size=1):
                                device=_dev())
 
 
-def run_gpu(s, albedo=None, shading=None, with_target=False, image_filter_size=1):
+def run_gpu(s, albedo=None, shading=None, with_target=False, image_filter_size=1, flags=0):
     import torch
     from gvr import renderer
     h = _handle(s, albedo, shading, image_filter_size)
@@ -50,7 +50,8 @@ def run_gpu(s, albedo=None, shading=None, with_target=False, image_filter_size=1
                                                         t["sh_coeff"], t["extrinsics"], t["intrinsics"])
     g = renderer.render_backward(h, t["grad_render"], t["vertex_pos"], t["vertex_color"], t["texture"],
                                  t["sh_coeff"], t["target_image"], vn, bary, face,
-                                 t["grad_target"] if with_target else None, t["extrinsics"], t["intrinsics"])
+                                 t["grad_target"] if with_target else None, t["extrinsics"], t["intrinsics"],
+                                 flags)
     rays = h.debug_rays(t["extrinsics"], t["intrinsics"])
     torch.cuda.synchronize()
     cpu = lambda x: x.cpu().numpy()
@@ -59,7 +60,7 @@ def run_gpu(s, albedo=None, shading=None, with_target=False, image_filter_size=1
                 sh_coeff_grad=cpu(g[3]))
 
 
-def check_batch(s, gpu, albedo=None, shading=None, with_target=False, image_filter_size=1, grads=True):
+def check_batch(s, gpu, albedo=None, shading=None, with_target=False, image_filter_size=1, grads=True, flags=0):
     B = s["vertex_pos"].shape[0]
     for b in range(B):
         o = oracle_scene(s, b, rays=gpu["rays"][b], albedo=albedo, shading=shading,
@@ -74,7 +75,8 @@ def check_batch(s, gpu, albedo=None, shading=None, with_target=False, image_filt
         if not grads:
             continue
         gt = s["grad_target"][b] if with_target else np.zeros_like(s["grad_target"][b])
-        g = o.backward(ref["face"], ref["bary"], ref["vertex_normal"], s["grad_render"][b], s["target_image"][b], gt)
+        g = o.backward(ref["face"], ref["bary"], ref["vertex_normal"], s["grad_render"][b], s["target_image"][b], gt,
+                       flags=flags)
         for k in ("vertex_pos_grad", "vertex_color_grad", "texture_grad", "sh_coeff_grad"):
             if np.all(g[k] == 0):
                 assert np.all(gpu[k][b] == 0), k
@@ -93,6 +95,19 @@ def test_modes_small_batch(albedo, shading):
     s["sh_coeff"][1] = s["sh_coeff"][1][::-1].copy()
     gpu = run_gpu(s)
     check_batch(s, gpu)
+
+
+@pytest.mark.parametrize("shading", ["shaded", "shadeless"])
+def test_albedo_position_option(shading):
+    """GVR_BACKWARD_ALBEDO_POSITION (no reference counterpart): the position
+    gradient also carries the vertex colour's change through the
+    barycentrics; GPU against the oracle's restatement of the same option."""
+    s = small_scene(num_faces=1280, views=2, size=64, albedo="vertexColor", shading=shading, seed=21, batch=2)
+    gpu = run_gpu(s, flags=1)
+    check_batch(s, gpu, flags=1)
+    base = run_gpu(s)
+    assert not np.allclose(base["vertex_pos_grad"], gpu["vertex_pos_grad"])
+    assert np.allclose(base["vertex_color_grad"], gpu["vertex_color_grad"], rtol=1e-5, atol=1e-7)
 
 
 def test_target_image_term():

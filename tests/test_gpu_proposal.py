@@ -1,0 +1,40 @@
+"""Learned proposal (gvr.proposal): a short training run on renders from
+this rasteriser must lower the network's loss, and on held-out parameter
+draws the trained proposal must start the fit closer to the ground truth
+than the mean does (lower photometric RMSE at step 0, lower parameter
+error) -- what the network gains over the fit without it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_proposal_trains_and_beats_the_mean_start():
+    import torch
+    from gvr import fitting, proposal, tc
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    model = fitting.MorphableModel(num_vertices=2562, seed=0, device=dev)
+    net = proposal.ProposalNet(dev, seed=0)
+    trainer = proposal.Trainer(model, net, batch=64, lr=1e-3, seed=1)
+    losses, secs = trainer.train(300, log_every=50)
+    assert tc.tc_error() == 0
+    first, last = losses[0][1], losses[-1][1]
+    assert last < 0.95 * first, losses
+
+    fitter = fitting.Fitter(model, num_views=4, size=128)
+    seeds = list(range(10_000, 10_016))
+    gt = np.concatenate([fitting.sample_params(np.random.default_rng(s), 1) for s in seeds])
+    p = torch.from_numpy(gt).to(dev)
+    with torch.no_grad():
+        target = fitter.render(p)
+        pred = net.predict(proposal.mosaic(trainer.view_fitter.render(p)))
+        mean = torch.from_numpy(fitting.mean_params(len(seeds))).to(dev)
+        rm_pred = torch.sqrt(fitter.loss(fitter.render(pred), target))
+        rm_mean = torch.sqrt(fitter.loss(fitter.render(mean), target))
+    sd = net.sd.clamp_min(1e-6)
+    active = net.sd > 0
+    err_pred = (((pred - p) / sd)[:, active] ** 2).mean()
+    err_mean = (((mean - p) / sd)[:, active] ** 2).mean()
+    assert float(err_pred) < float(err_mean)
+    assert float(rm_pred.mean()) < float(rm_mean.mean())

@@ -191,6 +191,37 @@ def test_fd_vertex_position_grad_constant_albedo():
     assert rel_norm(g["vertex_pos_grad"], fd) < 1e-4
 
 
+@pytest.mark.parametrize("shading", ["shaded", "shadeless"])
+def test_fd_vertex_position_grad_with_albedo_position_option(shading):
+    """Per-vertex colours: with the albedo-position option (flags=1) the
+    position gradient is the FP64 render's derivative; without it (the
+    reference) it is not."""
+    s = small_scene(num_faces=180, views=2, size=40, albedo="vertexColor", shading=shading, tex=8, seed=4)
+    o = oracle_scene(s)
+    out = o.forward()
+    _, flags = o.render_fp64(out["face"])
+    G = s["grad_render"][0].astype(np.float64)
+    G[flags != 0] = 0.0
+    G32 = G.astype(np.float32)
+    g1 = o.backward(out["face"], out["bary"], out["vertex_normal"], G32, s["target_image"][0], s["grad_target"][0],
+                    flags=1)["vertex_pos_grad"]
+    g0 = o.backward(out["face"], out["bary"], out["vertex_normal"], G32, s["target_image"][0], s["grad_target"][0],
+                    flags=0)["vertex_pos_grad"]
+    v0 = s["vertex_pos"][0].astype(np.float64)
+    h = 1e-4
+    fd = np.zeros_like(v0)
+    for i in range(v0.shape[0]):
+        for a in range(3):
+            vp, vm = v0.copy(), v0.copy()
+            vp[i, a] += h
+            vm[i, a] -= h
+            rp, _ = o.render_fp64(out["face"], vp)
+            rm, _ = o.render_fp64(out["face"], vm)
+            fd[i, a] = ((rp - rm) * G).sum() / (2 * h)
+    assert rel_norm(g1, fd) < 1e-4
+    assert rel_norm(g0, fd) > 1e-2
+
+
 def test_fd_vertex_color_and_sh_grads():
     s, o, out, G, g = _fd_setup("vertexColor")
     r0, _ = o.render_fp64(out["face"])
