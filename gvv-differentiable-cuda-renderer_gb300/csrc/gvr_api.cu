@@ -194,9 +194,9 @@ int gvr_create(const GvrTopology *topo, const GvrAttrs *attrs, GvrHandle **out) 
     if (attrs->render_resolution_v <= 0) return fail(GVR_ERR_INVALID_ARGUMENT, "render_resolution_v not set!");
     if (attrs->render_resolution_u > 32768 || attrs->render_resolution_v > 32768)
         return fail(GVR_ERR_INVALID_ARGUMENT, "render resolution above 32768");
-    if (attrs->albedo_mode < GVR_ALBEDO_VERTEX_COLOR || attrs->albedo_mode > GVR_ALBEDO_FOREGROUND_MASK)
+    if (attrs->albedo_mode < GVR_ALBEDO_VERTEX_COLOR || attrs->albedo_mode > GVR_ALBEDO_UV)
         return fail(GVR_ERR_INVALID_ARGUMENT, "INVALID ALBEDO MODE");
-    if (attrs->shading_mode != GVR_SHADING_SHADED && attrs->shading_mode != GVR_SHADING_SHADELESS)
+    if (attrs->shading_mode < GVR_SHADING_SHADED || attrs->shading_mode > GVR_SHADING_PHONG)
         return fail(GVR_ERR_INVALID_ARGUMENT, "INVALID SHADING MODE");
     // CudaRendererGrad.cpp:84-98
     if (attrs->image_filter_size <= 0) return fail(GVR_ERR_INVALID_ARGUMENT, "INVALID IMAGE FILTER SIZE");
@@ -302,7 +302,7 @@ static int check_forward_args(const GvrHandle *h, const GvrForwardArgs *a) {
     if (!batch_fits(h, a->batch))
         return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1 and the call within int32 index range");
     const int mode = h->attrs.albedo_mode;
-    const bool textured = mode == GVR_ALBEDO_TEXTURED;
+    const bool textured = mode == GVR_ALBEDO_TEXTURED || mode == GVR_ALBEDO_TEXTURED_BILINEAR;
     if (textured && (a->texture_height < 1 || a->texture_width < 1 || !a->texture))
         return fail(GVR_ERR_INVALID_ARGUMENT, "textured mode needs a texture of at least 1x1");
     if (!a->vertex_pos || !a->extrinsics || !a->intrinsics || !a->sh_coeff)
@@ -321,7 +321,8 @@ static int check_forward_args(const GvrHandle *h, const GvrForwardArgs *a) {
 
 // Texture size the forward uses (1x1 when neither textured nor normal-map).
 static void forward_texture_size(const GvrHandle *h, const GvrForwardArgs *a, int &Ht, int &Wt) {
-    const bool used = h->attrs.albedo_mode == GVR_ALBEDO_TEXTURED || h->attrs.compute_normal_map;
+    const bool used = h->attrs.albedo_mode == GVR_ALBEDO_TEXTURED || h->attrs.albedo_mode == GVR_ALBEDO_TEXTURED_BILINEAR ||
+                      h->attrs.compute_normal_map;
     Ht = used ? a->texture_height : 1;
     Wt = used ? a->texture_width : 1;
 }
@@ -383,12 +384,12 @@ int gvr_backward(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
     const int B = a->batch;
     if (!batch_fits(h, B)) return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1 and the call within int32 index range");
     const int mode = h->attrs.albedo_mode;
-    const bool textured = mode == GVR_ALBEDO_TEXTURED;
+    const bool textured = mode == GVR_ALBEDO_TEXTURED || mode == GVR_ALBEDO_TEXTURED_BILINEAR;
     if (a->texture_height < 1 || a->texture_width < 1)
         return fail(GVR_ERR_INVALID_ARGUMENT, "texture_height/texture_width must be >= 1 (texture_grad shape)");
     if (!a->vertex_pos_grad || !a->vertex_color_grad || !a->texture_grad || !a->sh_coeff_grad)
         return fail(GVR_ERR_INVALID_ARGUMENT, "all four gradient outputs are required");
-    const bool zeroMode = mode == GVR_ALBEDO_NORMAL || mode == GVR_ALBEDO_LIGHTING;
+    const bool zeroMode = mode == GVR_ALBEDO_NORMAL || mode == GVR_ALBEDO_LIGHTING || mode == GVR_ALBEDO_UV;
     if (!zeroMode) {
         if (!a->render_grad || !a->vertex_pos || !a->sh_coeff || !a->vertex_normal || !a->face || !a->extrinsics ||
             !a->intrinsics)

@@ -75,6 +75,7 @@ struct BwdIO {
     const float *grad_target;  // [B,C,H,W,3] or null
     float *tex_grad;           // [B,Ht,Wt,3]
     int imageFilter;
+    int phong;                 // GVR_SHADING_PHONG: albedo scaled by the headlight term, no SH
 };
 
 // ALBPOS (vertexColor only, opt-in): add the change of the interpolated
@@ -136,6 +137,10 @@ __global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, co
             float basis[9];
             sh_basis(n, basis);
             float JCoAl[3] = {1.0f, 1.0f, 1.0f};
+            if (!SHADED && io.phong) {  // d(colour)/d(albedo) of the headlight Phong term
+                const float k = phong_factor(-(n.x * d.x + n.y * d.y + n.z * d.z));
+                JCoAl[0] = JCoAl[1] = JCoAl[2] = k;
+            }
             if (SHADED) {
 #pragma unroll
                 for (int ch = 0; ch < 3; ++ch) {
@@ -171,6 +176,22 @@ __global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, co
                     atomicAdd(tg + 0, G[0] * JCoAl[0]);
                     atomicAdd(tg + 1, G[1] * JCoAl[1]);
                     atomicAdd(tg + 2, G[2] * JCoAl[2]);
+                }
+            }
+            if (MODE == GVR_ALBEDO_TEXTURED_BILINEAR) {  // the lookup and its derivative: four texels
+                const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+                int idx[4];
+                float w[4];
+                bilinear_taps(tc.x, tc.y, dims.Wt, dims.Ht, idx, w);
+                const float *tex = io.texture + (size_t)b * dims.Ht * dims.Wt * 3;
+                float *tgb = io.tex_grad + (size_t)b * dims.Ht * dims.Wt * 3;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+#pragma unroll
+                    for (int ch = 0; ch < 3; ++ch) {
+                        alb[ch] += w[k] * tex[3 * (size_t)idx[k] + ch];
+                        atomicAdd(tgb + 3 * (size_t)idx[k] + ch, w[k] * (G[ch] * JCoAl[ch]));
+                    }
                 }
             }
             // Pv: per-pixel vector applied with the stored barycentrics (target term);
@@ -480,8 +501,8 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     const int B = dims.B, C = dims.C, N = topo.N, F = topo.F, T = dims.tilesX * dims.tilesY;
     const size_t texBytes = (size_t)B * dims.Ht * dims.Wt * 3 * sizeof(float);
     cudaError_t err;
-    if (dims.albedo == GVR_ALBEDO_NORMAL || dims.albedo == GVR_ALBEDO_LIGHTING) {
-        // python/CudaRenderer.py:207-213: zero gradients for these modes
+    if (dims.albedo == GVR_ALBEDO_NORMAL || dims.albedo == GVR_ALBEDO_LIGHTING || dims.albedo == GVR_ALBEDO_UV) {
+        // python/CudaRenderer.py:207-213: zero gradients for these modes (and for the UV mode)
         if ((err = cudaMemsetAsync(a.vertex_pos_grad, 0, (size_t)B * N * 3 * sizeof(float), st))) return err;
         if ((err = cudaMemsetAsync(a.vertex_color_grad, 0, (size_t)B * N * 3 * sizeof(float), st))) return err;
         if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
@@ -493,8 +514,9 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
     if ((err = launch_cameras(a.extrinsics, a.intrinsics, ws.cams, B * C, st))) return err;
     if ((err = launch_face_geo(a.vertex_pos, topo, ws.geo, nullptr, B, st))) return err;
+    const int phong = dims.shading == GVR_SHADING_PHONG && dims.albedo != GVR_ALBEDO_FOREGROUND_MASK;
     BwdIO io{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image, a.vertex_normal,
-             a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter};
+             a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter, phong};
     const bool albpos = (a.flags & GVR_BACKWARD_ALBEDO_POSITION) != 0;
     switch (dims.albedo) {
         case GVR_ALBEDO_VERTEX_COLOR:
@@ -502,6 +524,9 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
             break;
         case GVR_ALBEDO_TEXTURED:
             err = launch_pixels_m<GVR_ALBEDO_TEXTURED>(shaded, target, false, topo, dims, ws, io, st);
+            break;
+        case GVR_ALBEDO_TEXTURED_BILINEAR:
+            err = launch_pixels_m<GVR_ALBEDO_TEXTURED_BILINEAR>(shaded, target, false, topo, dims, ws, io, st);
             break;
         default: err = launch_pixels_m<GVR_ALBEDO_FOREGROUND_MASK>(false, target, false, topo, dims, ws, io, st); break;
     }

@@ -219,6 +219,41 @@ __device__ __forceinline__ void sh_basis(V3 n, float basis[9]) {
     basis[8] = n.x * n.x - n.y * n.y;
 }
 
+// ---------------------------------------------------------------------------- modes without reference counterpart
+
+// Headlight Phong (GVR_SHADING_PHONG): colour = albedo * phong_factor + phong_specular,
+// with ndl = n . l for l the unit direction to the camera.
+constexpr float kPhongAmbient = 0.2f, kPhongDiffuse = 0.7f, kPhongSpecular = 0.3f;
+__device__ __forceinline__ float phong_factor(float ndl) { return kPhongAmbient + kPhongDiffuse * fmaxf(ndl, 0.0f); }
+__device__ __forceinline__ float phong_specular(float ndl) {
+    float r = fmaxf(2.0f * ndl * ndl - 1.0f, 0.0f);  // (r . v) for the mirror direction r of l about n, v = l
+    r *= r;
+    r *= r;
+    r *= r;
+    r *= r;  // ^16
+    return kPhongSpecular * r;
+}
+
+// Bilinear lookup (GVR_ALBEDO_TEXTURED_BILINEAR) at the clamped texture
+// coordinate (U0, V0) of texel_coord: texel centres at integer + 0.5,
+// neighbour indices clamped to the texture.  idx: texel offsets (in texels)
+// of the four corners, w: their weights.
+__device__ __forceinline__ void bilinear_taps(float U0, float V0, int Wt, int Ht, int idx[4], float w[4]) {
+    const float x = U0 - 0.5f, y = V0 - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    const int ix0 = min(max((int)x0, 0), Wt - 1), ix1 = min(max((int)x0 + 1, 0), Wt - 1);
+    const int iy0 = min(max((int)y0, 0), Ht - 1), iy1 = min(max((int)y0 + 1, 0), Ht - 1);
+    idx[0] = iy0 * Wt + ix0;
+    idx[1] = iy0 * Wt + ix1;
+    idx[2] = iy1 * Wt + ix0;
+    idx[3] = iy1 * Wt + ix1;
+    w[0] = (1.0f - fx) * (1.0f - fy);
+    w[1] = fx * (1.0f - fy);
+    w[2] = (1.0f - fx) * fy;
+    w[3] = fx * fy;
+}
+
 // ---------------------------------------------------------------------------- error-free FP32
 
 // s + e == a + b exactly (Knuth's TwoSum).

@@ -389,13 +389,37 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         case GVR_ALBEDO_NORMAL:
             col = make_float3((1.0f + n.x) * 0.5f, (1.0f + n.y) * 0.5f, (1.0f + n.z) * 0.5f);
             break;
+        case GVR_ALBEDO_TEXTURED_BILINEAR: {
+            const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+            int idx[4];
+            float w[4];
+            bilinear_taps(tc.x, tc.y, dims.Wt, dims.Ht, idx, w);
+            const float *tex = io.texture + (size_t)b * dims.Ht * dims.Wt * 3;
+            col = make_float3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float *t = tex + 3 * (size_t)idx[k];
+                col = make_float3(col.x + w[k] * t[0], col.y + w[k] * t[1], col.z + w[k] * t[2]);
+            }
+            break;
+        }
+        case GVR_ALBEDO_UV: {
+            const float *t = topo.uvs + 6 * (size_t)f;
+            col = make_float3(abc.x * t[0] + abc.y * t[2] + abc.z * t[4], abc.x * t[1] + abc.y * t[3] + abc.z * t[5],
+                              0.0f);
+            break;
+        }
         default:
             col = make_float3(1.0f, 1.0f, 1.0f);
             break;
     }
-    const bool shaded = (dims.shading == GVR_SHADING_SHADED && dims.albedo != GVR_ALBEDO_NORMAL) ||
-                        dims.albedo == GVR_ALBEDO_LIGHTING;
-    if (shaded) {
+    const bool lit = dims.albedo != GVR_ALBEDO_NORMAL && dims.albedo != GVR_ALBEDO_UV;
+    const bool shaded = (dims.shading == GVR_SHADING_SHADED && lit) || dims.albedo == GVR_ALBEDO_LIGHTING;
+    if (dims.shading == GVR_SHADING_PHONG && lit && dims.albedo != GVR_ALBEDO_LIGHTING) {
+        const float ndl = -(n.x * d.x + n.y * d.y + n.z * d.z);
+        const float k = phong_factor(ndl), s = phong_specular(ndl);
+        col = make_float3(col.x * k + s, col.y * k + s, col.z * k + s);
+    } else if (shaded) {
         const float *sh = io.sh + (size_t)bc * 27;
         float basis[9];
         sh_basis(n, basis);

@@ -13,8 +13,10 @@ I32 = ctypes.c_int32
 OK = 0
 STATUS = {0: "GVR_OK", -1: "GVR_ERR_INVALID_ARGUMENT", -2: "GVR_ERR_CUDA", -3: "GVR_ERR_OUT_OF_MEMORY",
           -4: "GVR_ERR_WORKSPACE", -5: "GVR_ERR_UNSUPPORTED"}
-ALBEDO = {"vertexColor": 0, "textured": 1, "normal": 2, "lighting": 3, "foregroundMask": 4}
-SHADING = {"shaded": 0, "shadeless": 1}
+# the reference's modes, then texturedBilinear, uv and phong (include/gvr.h)
+ALBEDO = {"vertexColor": 0, "textured": 1, "normal": 2, "lighting": 3, "foregroundMask": 4, "texturedBilinear": 5,
+          "uv": 6}
+SHADING = {"shaded": 0, "shadeless": 1, "phong": 2}
 
 
 class GvrTopology(ctypes.Structure):
@@ -63,7 +65,7 @@ EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forw
            "gvr_backward_workspace_size", "gvr_last_error", "gvr_abi_version", "gvr_debug_rays",
            "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc",
            "gvr_plan_create", "gvr_plan_forward", "gvr_plan_forward_graph", "gvr_plan_tile_config",
-           "gvr_plan_destroy",
+           "gvr_plan_destroy", "gvr_image_gradient", "gvr_image_gaussian3x3",
            # include/gvr_nn.h
            "gvr_gemm_bf16", "gvr_tc_error", "gvr_im2col_3x3s2", "gvr_col2im_3x3s2", "gvr_nn_last_error")
 
@@ -119,6 +121,10 @@ def load(build_if_missing: bool = True):
     L.gvr_plan_tile_config.restype = ctypes.c_int
     L.gvr_plan_destroy.argtypes = [P]
     L.gvr_plan_destroy.restype = None
+    L.gvr_image_gradient.argtypes = [P, P, P, I32, I32, I32, P]
+    L.gvr_image_gradient.restype = ctypes.c_int
+    L.gvr_image_gaussian3x3.argtypes = [P, P, I32, I32, I32, P]
+    L.gvr_image_gaussian3x3.restype = ctypes.c_int
     _lib = L
     return L
 

@@ -45,7 +45,10 @@ def smooth_fields(unit, count, sigma, rng, waves=8, freq=2.0):
 
 
 class MorphableModel:
-    """Mean displaced sphere (num_vertices = F/2 + 2) plus `n_shape` shape
+    """Mean: a sphere of radius 1000 mm (num_vertices = F/2 + 2) displaced
+    along its normals by a smooth field of RMS 20 mm (per-vertex noise of that
+    size would make a golf ball whose shading changes chaotically with the
+    slightest shift, which no photometric fit can follow); plus `n_shape` shape
     bases (mm) and `n_albedo` albedo bases: smooth random fields whose values
     are N(0, shape_sigma_mm^2) and N(0, albedo_sigma^2) per vertex and
     coordinate (smooth rather than independent per vertex, so that a
@@ -57,7 +60,12 @@ class MorphableModel:
                  albedo_sigma=0.01, seed=0, device=None, constant_albedo=None):
         rng = np.random.default_rng(seed)
         F = 2 * num_vertices - 4
-        verts, faces, unit = scenes.displaced_sphere(F, 1000.0, 20.0, rng)
+        unit, faces = scenes.sphere_mesh(F)
+        faces = faces.astype(np.int32)
+        # the mean: the sphere displaced along its normals by a smooth field of RMS 20 mm
+        disp = smooth_fields(unit, 1, 20.0, rng)[0].reshape(-1, 3)[:, 0]
+        disp *= 20.0 / np.sqrt(np.mean(disp * disp))
+        verts = (unit * (1000.0 + disp)[:, None]).astype(np.float32)
         self.faces = faces
         self.uvs = scenes.spherical_uvs(unit, faces)
         self.N, self.F = verts.shape[0], faces.shape[0]

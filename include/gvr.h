@@ -43,16 +43,29 @@ typedef enum {
     GVR_ERR_UNSUPPORTED = -5       /* combination not supported by this build      */
 } GvrStatus;
 
-/* AlbedoMode / ShadingMode (cpp/src/Renderer/CUDABasedRasterizationInput.h:25-35). */
+/* AlbedoMode / ShadingMode (cpp/src/Renderer/CUDABasedRasterizationInput.h:25-35).
+ * Values 0-4 and shading 0-1 are the reference's.  The others have no
+ * reference counterpart:
+ *   GVR_ALBEDO_TEXTURED_BILINEAR  bilinear texture lookup at the same texture
+ *       coordinate (texel centres at integer + 0.5, indices clamped to the
+ *       texture); its texture gradient is the lookup's derivative (4 texels).
+ *   GVR_ALBEDO_UV  the interpolated per-corner (u, v) as red and green, blue
+ *       0, never shaded; zero gradients (like the normal mode).
+ *   GVR_SHADING_PHONG  a headlight Phong term instead of SH:
+ *       albedo * (0.2 + 0.7 max(0, n.l)) + 0.3 max(0, 2 (n.l)^2 - 1)^16 with
+ *       l the direction to the camera; gradients for vertex colours and
+ *       texture only (no SH, no position gradient). */
 typedef enum {
     GVR_ALBEDO_VERTEX_COLOR = 0,
     GVR_ALBEDO_TEXTURED = 1,
     GVR_ALBEDO_NORMAL = 2,
     GVR_ALBEDO_LIGHTING = 3,
-    GVR_ALBEDO_FOREGROUND_MASK = 4
+    GVR_ALBEDO_FOREGROUND_MASK = 4,
+    GVR_ALBEDO_TEXTURED_BILINEAR = 5,
+    GVR_ALBEDO_UV = 6
 } GvrAlbedoMode;
 
-typedef enum { GVR_SHADING_SHADED = 0, GVR_SHADING_SHADELESS = 1 } GvrShadingMode;
+typedef enum { GVR_SHADING_SHADED = 0, GVR_SHADING_SHADELESS = 1, GVR_SHADING_PHONG = 2 } GvrShadingMode;
 
 typedef struct GvrHandle GvrHandle;
 
@@ -188,6 +201,18 @@ int gvr_debug_rays(GvrHandle *handle, int32_t batch, const float *extrinsics, co
  * results; everything that must start at zero is cleared inside each call. */
 #define GVR_NOALLOC_SCRATCH_BYTES (32u << 20)
 int gvr_backward_noalloc(GvrHandle *handle, const GvrBackwardArgs *args, void *stream);
+
+/* ---- Image helpers: gradientImageKernel and gaussianImageKernel of the
+ * reference (cpp/src/Renderer/gradientImage.cu:8-55, host entry
+ * gradientImage :57-67), over a batch of float RGB images [B, H, W, 3].
+ * Gradient: 1/8-scaled 3x3 Sobel in x and y, zero where x < 1, y < 1,
+ * x >= W - 2 or y >= H - 2.  Blur: 3x3 binomial (1 2 1)^2 / 16; the border
+ * ring (x < 1, y < 1, x > W - 2, y > H - 2) of `out` is not written.  The
+ * reference writes past the image when W or H is not a multiple of 16;
+ * these never do.  Asynchronous on `stream`. */
+int gvr_image_gradient(const float *image, float *grad_x, float *grad_y, int32_t batch, int32_t width,
+                       int32_t height, void *stream);
+int gvr_image_gaussian3x3(const float *image, float *out, int32_t batch, int32_t width, int32_t height, void *stream);
 
 /* ---- Batched forward of many meshes (no reference counterpart: the
  * reference renders one mesh per op call and loops over the batch on the

@@ -43,8 +43,9 @@
 
 #define ORC_MAX_TIES 4
 
-enum { ORC_VERTEX_COLOR = 0, ORC_TEXTURED = 1, ORC_NORMAL = 2, ORC_LIGHTING = 3, ORC_FOREGROUND = 4 };
-enum { ORC_SHADED = 0, ORC_SHADELESS = 1 };
+enum { ORC_VERTEX_COLOR = 0, ORC_TEXTURED = 1, ORC_NORMAL = 2, ORC_LIGHTING = 3, ORC_FOREGROUND = 4,
+       ORC_TEXTURED_BILINEAR = 5, ORC_UV = 6 };
+enum { ORC_SHADED = 0, ORC_SHADELESS = 1, ORC_PHONG = 2 };
 
 typedef struct {
     int N, F, C, W, H, Ht, Wt;
@@ -350,6 +351,43 @@ static void tex_coord(const orc_scene *s, int f, f3 abc, float *U0, float *V0) {
     *V0 = fy;
 }
 
+/* Modes without reference counterpart (gvr.h): bilinear texture lookup,
+ * headlight Phong, UV colour. */
+static void bilinear_taps(float U0, float V0, int Wt, int Ht, int idx[4], double w[4]) {
+    float x = U0 - 0.5f, y = V0 - 0.5f;
+    float x0 = floorf(x), y0 = floorf(y);
+    double fx = (double)(x - x0), fy = (double)(y - y0);
+    int ix0 = (int)x0, iy0 = (int)y0, ix1 = ix0 + 1, iy1 = iy0 + 1;
+    ix0 = ix0 < 0 ? 0 : ix0 > Wt - 1 ? Wt - 1 : ix0;
+    ix1 = ix1 < 0 ? 0 : ix1 > Wt - 1 ? Wt - 1 : ix1;
+    iy0 = iy0 < 0 ? 0 : iy0 > Ht - 1 ? Ht - 1 : iy0;
+    iy1 = iy1 < 0 ? 0 : iy1 > Ht - 1 ? Ht - 1 : iy1;
+    idx[0] = iy0 * Wt + ix0; idx[1] = iy0 * Wt + ix1; idx[2] = iy1 * Wt + ix0; idx[3] = iy1 * Wt + ix1;
+    w[0] = (1.0 - fx) * (1.0 - fy); w[1] = fx * (1.0 - fy); w[2] = (1.0 - fx) * fy; w[3] = fx * fy;
+}
+
+static d3 bilinear_albedo(const orc_scene *s, float U0, float V0) {
+    int idx[4];
+    double w[4];
+    bilinear_taps(U0, V0, s->Wt, s->Ht, idx, w);
+    d3 c = dk3(0, 0, 0);
+    for (int k = 0; k < 4; ++k) c = dadd(c, dscale(w[k], ldd3(s->texture + 3 * (size_t)idx[k])));
+    return c;
+}
+
+static double phong_factor(double ndl) { return 0.2 + 0.7 * (ndl > 0.0 ? ndl : 0.0); }
+static double phong_specular(double ndl) {
+    double r = 2.0 * ndl * ndl - 1.0;
+    if (r < 0.0) r = 0.0;
+    r *= r; r *= r; r *= r; r *= r;
+    return 0.3 * r;
+}
+
+static d3 uv_colour(const orc_scene *s, int f, double a, double b, double c) {
+    const float *t = s->uvs + (size_t)f * 6;
+    return dk3(a * t[0] + b * t[2] + c * t[4], a * t[1] + b * t[3] + c * t[5], 0.0);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Forward */
 
@@ -479,13 +517,24 @@ void orc_forward(const orc_scene *s, int32_t *face_out, float *bary_out, double 
                         col = dadd(dadd(dscale(abc.x, c0), dscale(abc.y, c1)), dscale(abc.z, c2));
                     } else if (s->albedo_mode == ORC_NORMAL) {
                         col = dk3((1.0 + n.x) / 2.0, (1.0 + n.y) / 2.0, (1.0 + n.z) / 2.0);
+                    } else if (s->albedo_mode == ORC_TEXTURED_BILINEAR) {
+                        float U0, V0;
+                        tex_coord(s, f, abc, &U0, &V0);
+                        col = bilinear_albedo(s, U0, V0);
+                    } else if (s->albedo_mode == ORC_UV) {
+                        col = uv_colour(s, f, abc.x, abc.y, abc.z);
                     } else {
                         col = dk3(1, 1, 1);
                     }
-                    int shaded = (s->shading_mode == ORC_SHADED && s->albedo_mode != ORC_NORMAL) ||
-                                 s->albedo_mode == ORC_LIGHTING;
+                    int lit = s->albedo_mode != ORC_NORMAL && s->albedo_mode != ORC_UV;
+                    int shaded = (s->shading_mode == ORC_SHADED && lit) || s->albedo_mode == ORC_LIGHTING;
                     if (s->albedo_mode == ORC_FOREGROUND) shaded = 0; /* forced shadeless, CudaRenderer.cpp:72-76 */
-                    if (shaded) {
+                    if (s->shading_mode == ORC_PHONG && lit && s->albedo_mode != ORC_LIGHTING &&
+                        s->albedo_mode != ORC_FOREGROUND) {
+                        double ndl = -ddot(n, f2d(d));
+                        double k = phong_factor(ndl), sp = phong_specular(ndl);
+                        col = dk3(col.x * k + sp, col.y * k + sp, col.z * k + sp);
+                    } else if (shaded) {
                         d3 l = sh_light(n, sh);
                         col = dk3(l.x * col.x, l.y * col.y, l.z * col.z);
                     }
@@ -709,7 +758,11 @@ void orc_backward_ex(const orc_scene *s, const int32_t *face, const float *bary,
     memset(gtex, 0, sizeof(double) * 3 * (size_t)s->Ht * s->Wt);
     memset(gsh, 0, sizeof(double) * 27 * C);
     const int shaded = s->shading_mode == ORC_SHADED && s->albedo_mode != ORC_FOREGROUND;
-    if (s->albedo_mode == ORC_NORMAL || s->albedo_mode == ORC_LIGHTING) { free_csr(&csr); return; }
+    if (s->albedo_mode == ORC_NORMAL || s->albedo_mode == ORC_LIGHTING || s->albedo_mode == ORC_UV) {
+        free_csr(&csr);
+        return;
+    }
+    const int phong = s->shading_mode == ORC_PHONG && s->albedo_mode != ORC_FOREGROUND;
     int nthreads = 1;
 #ifdef _OPENMP
     nthreads = omp_get_max_threads();
@@ -759,9 +812,14 @@ void orc_backward_ex(const orc_scene *s, const int32_t *face, const float *bary,
                     if (flipped) n = dscale(-1.0, n);
                     if (s->albedo_mode == ORC_FOREGROUND) Col[0] = Col[1] = Col[2] = dk3(1, 1, 1);
                     float U0 = 0.0f, V0 = 0.0f;
-                    if (s->albedo_mode == ORC_TEXTURED) tex_coord(s, f, abc, &U0, &V0);
+                    if (s->albedo_mode == ORC_TEXTURED || s->albedo_mode == ORC_TEXTURED_BILINEAR)
+                        tex_coord(s, f, abc, &U0, &V0);
                     d3 light = sh_light(n, sh);
                     m33 JCoAl = shaded ? m33_diag(light) : m33_ident();
+                    if (phong) {
+                        double k = phong_factor(-ddot(n, d));
+                        JCoAl = m33_diag(dk3(k, k, k));
+                    }
                     d3 alb = dk3(0, 0, 0);
                     int LUi = 0, LVi = 0;
                     if (s->albedo_mode == ORC_VERTEX_COLOR) {
@@ -779,6 +837,12 @@ void orc_backward_ex(const orc_scene *s, const int32_t *face, const float *bary,
                         double u0 = U0, v0 = V0;
                         alb = dadd(dscale(v0 - LV, dadd(dscale(u0 - LU, cLL), dscale(HU - u0, cHL))),
                                    dscale(HV - v0, dadd(dscale(u0 - LU, cLH), dscale(HU - u0, cHH))));
+                    }
+                    int bidx[4] = {0, 0, 0, 0};
+                    double bw[4] = {0, 0, 0, 0};
+                    if (s->albedo_mode == ORC_TEXTURED_BILINEAR) {
+                        bilinear_taps(U0, V0, s->Wt, s->Ht, bidx, bw);
+                        alb = bilinear_albedo(s, U0, V0);
                     }
                     m33 JCoLi = m33_diag(alb);
                     const float *gr = grad_render + 3 * p;
@@ -800,6 +864,17 @@ void orc_backward_ex(const orc_scene *s, const int32_t *face, const float *bary,
                         dst[1] += gt.y;
 #pragma omp atomic
                         dst[2] += gt.z;
+                    } else if (s->albedo_mode == ORC_TEXTURED_BILINEAR) {
+                        d3 gt = rowmul(G, JCoAl);
+                        for (int k = 0; k < 4; ++k) {
+                            double *dst = gtex + 3 * (size_t)bidx[k];
+#pragma omp atomic
+                            dst[0] += bw[k] * gt.x;
+#pragma omp atomic
+                            dst[1] += bw[k] * gt.y;
+#pragma omp atomic
+                            dst[2] += bw[k] * gt.z;
+                        }
                     }
                     /* SH (:402-436) */
                     if (shaded) {
@@ -993,13 +1068,38 @@ void orc_render_fp64_ex(const orc_scene *s, const double *verts_d, const double 
                     col = dadd(dadd(dscale(a, CD(i0)), dscale(b, CD(i1))), dscale(cc, CD(i2)));
                 } else if (s->albedo_mode == ORC_NORMAL) {
                     col = dk3((1.0 + n.x) / 2.0, (1.0 + n.y) / 2.0, (1.0 + n.z) / 2.0);
+                } else if (s->albedo_mode == ORC_TEXTURED_BILINEAR) {
+                    const float *tt = s->uvs + (size_t)f * 6;
+                    double U = (tt[0] * a + tt[2] * b + tt[4] * cc) * s->Wt;
+                    double V = ((1.0 - tt[1]) * a + (1.0 - tt[3]) * b + (1.0 - tt[5]) * cc) * s->Ht;
+                    U = fmin(fmax(U, 0.0), s->Wt - 1.0) - 0.5;
+                    V = fmin(fmax(V, 0.0), s->Ht - 1.0) - 0.5;
+                    double x0 = floor(U), y0 = floor(V), fx = U - x0, fy = V - y0;
+                    int ix[2] = {(int)x0, (int)x0 + 1}, iy[2] = {(int)y0, (int)y0 + 1};
+                    for (int k = 0; k < 2; ++k) {
+                        ix[k] = ix[k] < 0 ? 0 : ix[k] > s->Wt - 1 ? s->Wt - 1 : ix[k];
+                        iy[k] = iy[k] < 0 ? 0 : iy[k] > s->Ht - 1 ? s->Ht - 1 : iy[k];
+                    }
+                    col = dk3(0, 0, 0);
+                    for (int ky = 0; ky < 2; ++ky)
+                        for (int kx = 0; kx < 2; ++kx) {
+                            double w = (kx ? fx : 1.0 - fx) * (ky ? fy : 1.0 - fy);
+                            col = dadd(col, dscale(w, ldd3(s->texture + ((size_t)iy[ky] * s->Wt + ix[kx]) * 3)));
+                        }
+                } else if (s->albedo_mode == ORC_UV) {
+                    col = uv_colour(s, f, a, b, cc);
                 } else {
                     col = dk3(1, 1, 1);
                 }
-                int shaded = (s->shading_mode == ORC_SHADED && s->albedo_mode != ORC_NORMAL) ||
-                             s->albedo_mode == ORC_LIGHTING;
+                int lit = s->albedo_mode != ORC_NORMAL && s->albedo_mode != ORC_UV;
+                int shaded = (s->shading_mode == ORC_SHADED && lit) || s->albedo_mode == ORC_LIGHTING;
                 if (s->albedo_mode == ORC_FOREGROUND) shaded = 0;
-                if (shaded) {
+                if (s->shading_mode == ORC_PHONG && lit && s->albedo_mode != ORC_LIGHTING &&
+                    s->albedo_mode != ORC_FOREGROUND) {
+                    double ndl = -ddot(n, d);
+                    double k = phong_factor(ndl), sp = phong_specular(ndl);
+                    col = dk3(col.x * k + sp, col.y * k + sp, col.z * k + sp);
+                } else if (shaded) {
                     d3 l = sh_light_d(n, sh);
                     col = dk3(l.x * col.x, l.y * col.y, l.z * col.z);
                 }

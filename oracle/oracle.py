@@ -14,8 +14,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle.so")
 
-ALBEDO = {"vertexColor": 0, "textured": 1, "normal": 2, "lighting": 3, "foregroundMask": 4}
-SHADING = {"shaded": 0, "shadeless": 1}
+ALBEDO = {"vertexColor": 0, "textured": 1, "normal": 2, "lighting": 3, "foregroundMask": 4, "texturedBilinear": 5,
+          "uv": 6}
+SHADING = {"shaded": 0, "shadeless": 1, "phong": 2}
 
 
 class _Scene(ctypes.Structure):

@@ -86,6 +86,9 @@ def check_batch(s, gpu, albedo=None, shading=None, with_target=False, image_filt
 
 MODES = [(a, sh) for a in ("vertexColor", "textured", "normal", "lighting", "foregroundMask")
          for sh in ("shaded", "shadeless")]
+# modes without reference counterpart (include/gvr.h), pinned by the oracle's restatement
+MODES += [("texturedBilinear", "shaded"), ("texturedBilinear", "shadeless"), ("uv", "shaded"),
+          ("vertexColor", "phong"), ("textured", "phong"), ("texturedBilinear", "phong"), ("normal", "phong")]
 
 
 @pytest.mark.parametrize("albedo,shading", MODES)
@@ -107,7 +110,7 @@ def test_albedo_position_option(shading):
     check_batch(s, gpu, flags=1)
     base = run_gpu(s)
     assert not np.allclose(base["vertex_pos_grad"], gpu["vertex_pos_grad"])
-    assert np.allclose(base["vertex_color_grad"], gpu["vertex_color_grad"], rtol=1e-5, atol=1e-7)
+    assert rel_norm(gpu["vertex_color_grad"], base["vertex_color_grad"]) <= 1e-6   # float atomics reorder sums
 
 
 def test_target_image_term():

@@ -262,6 +262,40 @@ def test_fd_texture_grad():
     assert rel_norm(g["texture_grad"], fd) < 1e-5
 
 
+@pytest.mark.parametrize("shading", ["shaded", "phong"])
+def test_fd_bilinear_texture_grad(shading):
+    """texturedBilinear (no reference counterpart): the texture gradient is
+    the bilinear lookup's derivative on every covered pixel."""
+    s, o, out, G, g = _fd_setup("texturedBilinear", shading=shading)
+    r0, _ = o.render_fp64(out["face"])
+    tex = s["texture"][0].astype(np.float64)
+    fd = np.zeros_like(tex)
+    for y in range(tex.shape[0]):
+        for x in range(tex.shape[1]):
+            for a in range(3):
+                t2 = tex.copy()
+                t2[y, x, a] += 0.25
+                r1, _ = o.with_(texture=t2).render_fp64(out["face"])
+                fd[y, x, a] = ((r1 - r0) * G).sum() / 0.25
+    assert np.linalg.norm(fd) > 0
+    assert rel_norm(g["texture_grad"], fd) < 1e-4
+
+
+def test_fd_phong_vertex_color_grad():
+    s, o, out, G, g = _fd_setup("vertexColor", shading="phong")
+    r0, _ = o.render_fp64(out["face"])
+    col = s["vertex_color"][0].astype(np.float64)
+    fd = np.zeros_like(col)
+    for i in range(col.shape[0]):
+        for a in range(3):
+            c2 = col.copy()
+            c2[i, a] += 0.25
+            r1, _ = o.with_(colors=c2).render_fp64(out["face"])
+            fd[i, a] = ((r1 - r0) * G).sum() / 0.25
+    assert rel_norm(g["vertex_color_grad"], fd) < 1e-5
+    assert np.all(g["sh_coeff_grad"] == 0) and np.all(g["vertex_pos_grad"] == 0)
+
+
 def test_bary_jacobian_closed_form_matches_restatement():
     """The kernels use d(bary)/d(v_j) = -b_j [g1, g2, -(g1+g2)] with
     g1 = (e2 x d)/(N.d), g2 = (d x e1)/(N.d); the oracle restates the
