@@ -82,7 +82,7 @@ struct BwdIO {
 // vertex colour through the barycentrics to the position gradient, which the
 // reference leaves out (CUDABasedRasterizationGrad.cu:489).
 template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
-__global__ void __launch_bounds__(kTilePix) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
+__global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
                                                          const BwdIO io) {
     constexpr bool COL = MODE == GVR_ALBEDO_VERTEX_COLOR;
     constexpr bool POS = SHADED || TARGET || ALBPOS;

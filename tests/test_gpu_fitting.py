@@ -122,16 +122,21 @@ def test_fit_gradient_shape_and_pose_match_fd_with_albedo_term():
 
 def test_fit_recovers_lighting():
     """From the true geometry, pose and albedo with the mean lighting, 150
-    Adam steps (geometry step sizes small, as for a refinement) cut the
-    photometric RMSE to under a third, steadily, and the fit records the
-    RMSE and GPU time of every step."""
+    Adam steps on the SH coefficients alone (every other step size zero,
+    no decay) cut the photometric RMSE to under a fifth, steadily, and the
+    fit records the RMSE and GPU time of every step.  (With geometry and
+    albedo free as well, they drift to absorb the wrong shading and the
+    RMSE stalls near 0.04: the lighting is identified only with the rest
+    held.)"""
     model, fitter, gt, target = _setup(seed=5)
     init = gt.copy()
     init[:, 166:193] = 0.0
     init[:, [166, 175, 184]] = 0.85
-    res = fitter.fit(target, init, steps=150, goal=0.01, lr=dict(shape=0.005, rot=0.001, trans=0.5))
+    frozen = dict(shape=0.0, albedo=0.0, rot=0.0, trans=0.0)
+    res = fitter.fit(target, init, steps=150, goal=0.001, lr=frozen, decay=1.0)
     r = res.rmse[:, 0]
     assert r[0] > 0.03
-    assert r[-1] < r[0] / 3, r[::10]
+    assert r[-1] < r[0] / 5, r[::10]
+    assert np.allclose(res.params[0, :166], gt[0, :166])
     assert np.all(r[10::10] <= r[:-10:10] * 1.05), r[::10]   # no divergence
     assert res.step_ms.shape == (151,) and np.all(np.diff(res.step_ms) >= 0)

@@ -70,8 +70,10 @@ def test_workloads_match_reference_kernels(ref_nofma, ref_default):
         _, ties = compare_visibility(s, ours, ref, "workload")
         d = ref_default.forward(s)
         mism = (d["face"] != ours["face"][0]).mean()
+        g = ref_default.backward(s, d)
         print(f"\n{s['num_views']}x{s['width']}^2, F={s['faces'].shape[0]}: tie pixels {ties}, "
-              f"default-build (FMA) face mismatch rate {mism:.2e}, ref kernels {ref['ms']:.2f} ms")
+              f"default-build (FMA) face mismatch rate {mism:.2e}, reference kernels: forward "
+              f"{d['ms']:.2f} ms, backward {g['ms']:.2f} ms (default build), forward {ref['ms']:.2f} ms (-fmad=false)")
         assert mism < 0.01
 
 
