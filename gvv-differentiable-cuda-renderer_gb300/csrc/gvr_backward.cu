@@ -62,6 +62,22 @@ __device__ __forceinline__ void group_reduce(float (&val)[NV], unsigned peers, i
     }
 }
 
+// One butterfly step of a warp reduce-scatter: each lane carries C partial
+// sums, swaps half of them with the lane C/2 away and keeps C/2.  Steps
+// C = 32, 16, 8, 4, 2 leave lane k with the warp's sum of value k, in
+// 16+8+4+2+1 = 31 shuffles (a shuffle tree per value takes 32 x 5).
+template <int C>
+__device__ __forceinline__ void reduce_scatter_step(float (&r)[32], int lane) {
+    constexpr int H = C / 2;
+    const bool upper = (lane & H) != 0;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+        const float send = upper ? r[i] : r[i + H];
+        const float keep = upper ? r[i + H] : r[i];
+        r[i] = keep + __shfl_xor_sync(0xffffffffu, send, H);
+    }
+}
+
 struct BwdIO {
     const float *grad_render;  // [B,C,H,W,3]
     const float *verts;        // [B,N,3]
@@ -103,9 +119,9 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
     float val[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) val[k] = 0.0f;
-    float shv[SHADED ? 27 : 1];
+    float shv[SHADED ? 32 : 1];  // 27 SH terms, padded to a warp for the reduce-scatter
 #pragma unroll
-    for (int k = 0; k < (SHADED ? 27 : 1); ++k) shv[k] = 0.0f;
+    for (int k = 0; k < (SHADED ? 32 : 1); ++k) shv[k] = 0.0f;
 
     if (f >= 0) {
         const Camera &cam = ws.cams[bc];
@@ -329,6 +345,18 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
         }
     }
 
+    // ---- SH partial sums of this tile: warp part first, which frees the
+    // 32 per-lane terms before the face reduction needs its registers
+    __shared__ float red[kTilePix / 32][27];
+    if constexpr (SHADED) {
+        reduce_scatter_step<32>(shv, lane);
+        reduce_scatter_step<16>(shv, lane);
+        reduce_scatter_step<8>(shv, lane);
+        reduce_scatter_step<4>(shv, lane);
+        reduce_scatter_step<2>(shv, lane);
+        if (lane < 27) red[warp][lane] = shv[0];
+    }
+
     // ---- per-face pre-reduction and accumulation
     if (NPOS + NGN + NCOL > 0) {
         const unsigned peers = __match_any_sync(0xffffffffu, f);
@@ -360,16 +388,8 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
         }
     }
 
-    // ---- SH partial sums of this tile
-    if (SHADED) {
-        __shared__ float red[kTilePix / 32][27];
-#pragma unroll
-        for (int k = 0; k < 27; ++k) {
-            float x = shv[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) red[warp][k] = x;
-        }
+    // ---- SH partial sums of this tile (block part)
+    if constexpr (SHADED) {
         __syncthreads();
         if (tid < 27) {
             float s = 0.0f;

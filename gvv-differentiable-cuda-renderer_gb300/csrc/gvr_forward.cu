@@ -271,41 +271,44 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
 }
 
 // Exclusive scan of n counts by one 1024-thread block; start[n] = total.
+// Exclusive scan of count[0..n) into start[0..n], start[n] = total, by one
+// block of 1024 threads: each thread sums a contiguous run of ceil(n/1024)
+// counts, one block scan of the run sums, then each thread writes its run.
+// (Two passes over the counts and two barriers, instead of a block scan per
+// 1024 counts.)
 __device__ __forceinline__ void scan_block(const int *__restrict__ count, int *__restrict__ start, int n) {
     __shared__ int warpSum[32];
-    __shared__ int carry;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) carry = 0;
+    const int per = (n + 1023) / 1024;
+    const int lo = min(n, tid * per), hi = min(n, lo + per);
+    int sum = 0;
+    for (int i = lo; i < hi; ++i) sum += count[i];
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warpSum[warp] = incl;
     __syncthreads();
-    for (int base = 0; base < n; base += 1024) {
-        int idx = base + tid;
-        int x = idx < n ? count[idx] : 0;
-        int incl = x;
+    if (warp == 0) {
+        const int w = warpSum[lane];
+        int wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+            const int y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
         }
-        if (lane == 31) warpSum[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            int w = warpSum[lane];
-            int wi = w;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, wi, o);
-                if (lane >= o) wi += y;
-            }
-            warpSum[lane] = wi - w;  // exclusive prefix of warp sums
-        }
-        __syncthreads();
-        int excl = carry + warpSum[warp] + incl - x;
-        if (idx < n) start[idx] = excl;
-        __syncthreads();
-        if (tid == 1023) carry = excl + x;
-        __syncthreads();
+        warpSum[lane] = wi - w;  // exclusive prefix of warp sums
     }
-    if (tid == 0) start[n] = carry;
+    __syncthreads();
+    int run = warpSum[warp] + incl - sum;
+    for (int i = lo; i < hi; ++i) {
+        const int x = count[i];
+        start[i] = run;
+        run += x;
+    }
+    if (tid == 1023) start[n] = run;
 }
 
 __device__ __forceinline__ void bin_fill_item(const FwdJob &J, int i) {

@@ -29,18 +29,20 @@
 namespace gvr {
 namespace {
 
-constexpr int kCachedEntries = 320;  // compacted face entries of a tile kept in shared memory
-constexpr int kBuckets = 64;         // depth buckets of the front-to-back order
-constexpr int kMaxCand = 4;          // candidates a pixel keeps in registers
+constexpr int kChunk = kTilePix;  // face entries staged per pass: one per thread
+constexpr int kBuckets = 64;      // depth buckets of the front-to-back order
+constexpr int kMaxCand = 4;       // candidates a pixel keeps in registers
 
-// Face entry with its skip-test constants and its box clipped to the tile (80 bytes).
+// Face entry with its skip-test constants and its box clipped to the tile
+// (80 bytes).  Fields are grouped in 16-byte rows in the order the walk
+// tests them, so an entry rejected by its box costs one shared-memory load.
 struct __align__(16) Entry {
-    float x0, y0, a1, b1;
-    float a2, b2, r0, r1;
-    float r2, mIn, mOut, dRel;
-    float zLowSafe;
-    int flags, f, pad;
     int bx0, by0, bx1, by1;
+    float zLowSafe, mOut;
+    int flags, f;
+    float x0, y0, a1, b1;
+    float a2, b2, mIn, dRel;
+    float r0, r1, r2, pad;
 };
 
 __device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX0, int tileY0, int tileW, int tileH) {
@@ -60,7 +62,7 @@ __device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX
     E.zLowSafe = vf.s0.w;
     E.flags = vf_flags(vf);
     E.f = f;
-    E.pad = 0;
+    E.pad = 0.0f;
     const int4 box = vf_box(vf);
     E.bx0 = max(box.x, tileX0);
     E.by0 = max(box.y, tileY0);
@@ -71,17 +73,28 @@ __device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX
 
 // Screen barycentrics of pixel centre (px, py) and the depth estimate 1e4*S/T
 // (the reference's 1e4 / sum(b_i / z_i) with b_i its world barycentrics).
-__device__ __forceinline__ void entry_lambda(const Entry &E, float px, float py, float &l0, float &l1, float &l2) {
-    const float dx = px - E.x0, dy = py - E.y0;
-    l1 = E.a1 * dx + E.b1 * dy;
-    l2 = E.a2 * dx + E.b2 * dy;
+// g0 = (x0, y0, a1, b1), (a2, b2) of the entry.
+__device__ __forceinline__ void lambda_at(const float4 &g0, float a2, float b2, float px, float py, float &l0, float &l1,
+                                          float &l2) {
+    const float dx = px - g0.x, dy = py - g0.y;
+    l1 = g0.z * dx + g0.w * dy;
+    l2 = a2 * dx + b2 * dy;
     l0 = 1.0f - l1 - l2;
 }
 
-__device__ __forceinline__ float entry_depth(const Entry &E, float l0, float l1, float l2) {
-    const float S = l0 * E.r0 + l1 * E.r1 + l2 * E.r2;
-    const float T = l0 * E.r0 * E.r0 + l1 * E.r1 * E.r1 + l2 * E.r2 * E.r2;
+// r = (r0, r1, r2): reciprocal vertex depths.
+__device__ __forceinline__ float depth_at(const float4 &r, float l0, float l1, float l2) {
+    const float S = l0 * r.x + l1 * r.y + l2 * r.z;
+    const float T = l0 * r.x * r.x + l1 * r.y * r.y + l2 * r.z * r.z;
     return 10000.0f * __fdividef(S, T);
+}
+
+__device__ __forceinline__ void entry_lambda(const Entry &E, float px, float py, float &l0, float &l1, float &l2) {
+    lambda_at(make_float4(E.x0, E.y0, E.a1, E.b1), E.a2, E.b2, px, py, l0, l1, l2);
+}
+
+__device__ __forceinline__ float entry_depth(const Entry &E, float l0, float l1, float l2) {
+    return depth_at(make_float4(E.r0, E.r1, E.r2, 0.0f), l0, l1, l2);
 }
 
 // False when no pixel centre of the entry's clipped box can pass the
@@ -136,14 +149,21 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     const FrameDims &dims = J.dims;
     const FwdScratch &ws = J.ws;
     const RasterIO &io = J.io;
-    __shared__ Entry sE[kCachedEntries];
-    __shared__ int sCount;
+    __shared__ Entry sE[kChunk];
+    __shared__ float sBucketLo[kChunk];
+    __shared__ int sHist[kBuckets + 1];
+    __shared__ unsigned sKeyLo, sKeyHi;
     const int T = dims.tilesX * dims.tilesY;
     const int tile = item % T, bc = item / T, b = bc / dims.C;
     const int tileW = dims.tileW, tileH = dims.tileH;
     const int tileX0 = (tile % dims.tilesX) * tileW, tileY0 = (tile / dims.tilesX) * tileH;
-    const int tid = threadIdx.x;
-    const int u = tileX0 + (tid & (tileW - 1)), v = tileY0 + (tid >> dims.tileShift);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // Each warp owns an 8x4 block of the tile (tileW / 8 blocks across):
+    // fewer faces overlap it than a full-width strip of 32 pixels.
+    const int wAcross = tileW >> 3;
+    const int colLo = tileX0 + ((warp % wAcross) << 3), rowLo = tileY0 + ((warp / wAcross) << 2);
+    const int colHi = colLo + 7, rowHi = rowLo + 3;
+    const int u = colLo + (lane & 7), v = rowLo + (lane >> 3);
     const float px = u + 0.5f, py = v + 0.5f;
     const int F = topo.F;
     const ViewFace *VF = ws.vface + (size_t)bc * F;
@@ -151,24 +171,15 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     const size_t tIdx = (size_t)bc * T + tile;
     const int s0 = ws.tileStart[tIdx], nTile = ws.tileStart[tIdx + 1] - s0;
     const int nAll = nTile + ws.bigCount[bc];
-
-    const int lane = tid & 31;
-    // the pixel rows of this warp (32 / tileW rows of tileW pixels)
-    const int rowLo = tileY0 + ((tid & ~31) >> dims.tileShift), rowHi = rowLo + (32 >> dims.tileShift) - 1;
     const float kInf = __int_as_float(0x7f800000);
-    __shared__ float sKey[kCachedEntries];
-    __shared__ short sOrder[kCachedEntries];
-    __shared__ float sBucketLo[kCachedEntries];
-    __shared__ int sHist[kBuckets + 1];
-    __shared__ unsigned sKeyLo, sKeyHi;
 
     // One pass front to back: `zup` is the smallest certain depth bound so
     // far; candidates (face, lower depth bound) are kept while their bound
     // does not exceed it.  A bound only decreases, so a face dropped early
     // could never win; the survivors are filtered again by the final bound.
-    // The tile's entries go through shared memory in chunks of
-    // kCachedEntries (dense meshes at low resolution put thousands of faces
-    // in a tile); zup and the candidates carry over from chunk to chunk.
+    // The tile's entries go through shared memory in chunks of kChunk (dense
+    // meshes at low resolution put thousands of faces in a tile); zup and
+    // the candidates carry over from chunk to chunk.
     float zup = kInf;
     int nCand = 0;
     bool spill = false;
@@ -179,60 +190,42 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         cf[j] = -1;
         cz[j] = kInf;
     }
-    for (int c0 = 0; c0 < nAll; c0 += kCachedEntries) {
-    const int cEnd = min(nAll, c0 + kCachedEntries);
-    // stage the chunk's entries whose triangle may cover a pixel of the tile (compacted in any order)
-    if (tid == 0) sCount = 0;
-    __syncthreads();  // (also: every warp is done walking the previous chunk)
-    for (int e0 = c0; e0 < cEnd; e0 += kTilePix) {
-        const int e = e0 + tid;
+    if (tid == 0) {
+        sKeyLo = 0x7f800000u;
+        sKeyHi = 0u;
+    }
+    if (tid <= kBuckets) sHist[tid] = 0;
+    for (int c0 = 0; c0 < nAll; c0 += kChunk) {
+        // Each thread builds one entry of the chunk and keeps it in registers
+        // until its place in the front-to-back order is known: a counting
+        // sort into kBuckets depth buckets spanning the chunk's finite depth
+        // lower bounds (faces without a bound go first).  sBucketLo[i] is a
+        // lower bound of the depth bound of entry i and of every entry after
+        // it, which is all the early exit needs.
+        const int e = c0 + tid;
         bool keep = false;
         Entry E;
-        if (e < cEnd) {
+        if (e < nAll) {
             const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
             E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
             keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        int base = 0;
-        if (lane == 0 && m) base = atomicAdd(&sCount, __popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (keep) {
-            const int slot = base + __popc(m & ((1u << lane) - 1u));  // < cEnd - c0 <= kCachedEntries
-            sE[slot] = E;
-            sKey[slot] = E.zLowSafe;
-        }
-    }
-    __syncthreads();
-    const int nE = sCount;
-
-    // Front-to-back order: counting sort into kBuckets depth buckets spanning
-    // the chunk's finite depth lower bounds (faces without a bound go first).
-    // sBucketLo[i] is a lower bound of the depth bound of entry i and of
-    // every entry after it, which is all the early exit needs.
-    {
-        if (tid == 0) {
-            sKeyLo = 0x7f800000u;
-            sKeyHi = 0u;
-        }
-        if (tid <= kBuckets) sHist[tid] = 0;
-        __syncthreads();
-        for (int e = tid; e < nE; e += kTilePix) {
-            const float k = sKey[e];
-            if (k >= 0.0f && k < __int_as_float(0x7f800000)) {  // finite, non-negative: order like unsigned ints
-                atomicMin(&sKeyLo, __float_as_uint(k));
-                atomicMax(&sKeyHi, __float_as_uint(k));
-            }
+        // finite, non-negative bounds order like unsigned ints
+        const bool ranged = keep && E.zLowSafe >= 0.0f && E.zLowSafe < kInf;
+        const unsigned kLo = __reduce_min_sync(0xffffffffu, ranged ? __float_as_uint(E.zLowSafe) : 0x7f800000u);
+        const unsigned kHi = __reduce_max_sync(0xffffffffu, ranged ? __float_as_uint(E.zLowSafe) : 0u);
+        __syncthreads();  // every warp is done walking the previous chunk; the sort state is reset
+        if (lane == 0) {
+            atomicMin(&sKeyLo, kLo);
+            atomicMax(&sKeyHi, kHi);
         }
         __syncthreads();
         const float lo = __uint_as_float(sKeyLo), hi = __uint_as_float(sKeyHi);
         const float scale = hi > lo ? (float)kBuckets / (hi - lo) : 0.0f;
-        auto bucket_of = [&](float k) -> int {  // 0: no usable bound; 1..kBuckets by depth
-            if (!(k >= lo)) return 0;
-            return 1 + min(kBuckets - 1, (int)((k - lo) * scale));
-        };
-        for (int e = tid; e < nE; e += kTilePix) atomicAdd(&sHist[bucket_of(sKey[e])], 1);
-        __syncthreads();
+        // 0: no usable bound; 1..kBuckets by depth
+        const int q = !keep || !(E.zLowSafe >= lo) ? 0 : 1 + min(kBuckets - 1, (int)((E.zLowSafe - lo) * scale));
+        if (keep) atomicAdd(&sHist[q], 1);
+        const int nE = __syncthreads_count(keep);
         if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: 3 per lane, one warp scan
             const int q0 = 3 * tid;
             const int h0 = q0 <= kBuckets ? sHist[q0] : 0, h1 = q0 + 1 <= kBuckets ? sHist[q0 + 1] : 0,
@@ -250,63 +243,72 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             if (q0 + 2 <= kBuckets) sHist[q0 + 2] = ex + h0 + h1;
         }
         __syncthreads();
-        for (int e = tid; e < nE; e += kTilePix) {
-            const int q = bucket_of(sKey[e]);
-            const int pos = atomicAdd(&sHist[q], 1);
-            sOrder[pos] = (short)e;
+        if (keep) {
+            const int pos = atomicAdd(&sHist[q], 1);  // < nE <= kChunk
+            sE[pos] = E;
             // the bucket's lower edge, pulled down by 0.1% of its offset so rounding
-            // in bucket_of can never leave a member below it
-            sBucketLo[pos] = q == 0 ? -__int_as_float(0x7f800000) : q == 1 ? lo : lo + (float)(q - 1) * (0.999f / scale);
+            // in the bucket index can never leave a member below it
+            sBucketLo[pos] = q == 0 ? -kInf : q == 1 ? lo : lo + (float)(q - 1) * (0.999f / scale);
         }
-    }
-    __syncthreads();
+        __syncthreads();
+        // the sort state is free until the next chunk's first barrier
+        if (tid == 0) {
+            sKeyLo = 0x7f800000u;
+            sKeyHi = 0u;
+        }
+        if (tid <= kBuckets) sHist[tid] = 0;
 
-    for (int i = 0; i < nE; ++i) {
-        const Entry E = sE[sOrder[i]];
-        // every later entry of the chunk lies behind every pixel of this warp: stop
-        if (sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
-        if (E.by1 < rowLo || E.by0 > rowHi) continue;  // warp-uniform
-        if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
-        if (E.zLowSafe > zup) continue;  // behind this pixel's covering face (and so is every later entry)
-        float zlow = -kInf;
-        if (E.flags & kScreenValid) {
-            float l0, l1, l2;
-            entry_lambda(E, px, py, l0, l1, l2);
-            if (l0 < -E.mOut || l1 < -E.mOut || l2 < -E.mOut) continue;  // certainly outside
-            const float zq = entry_depth(E, l0, l1, l2);
-            if ((E.flags & kCertain) && l0 >= E.mIn && l1 >= E.mIn && l2 >= E.mIn)
-                zup = fminf(zup, zq * (1.0f + E.dRel) + 2.0f);
-            zlow = E.zLowSafe;
-            if (E.dRel < 0.25f) zlow = fmaxf(zlow, zq * (1.0f - E.dRel) - 2.0f);
-            if (zlow > zup) continue;  // certainly behind a covering face
-        }
-        if (nCand == kMaxCand) {  // make room: drop candidates now known to lose
-            int m = 0;
-#pragma unroll
-            for (int j = 0; j < kMaxCand; ++j) {
-                const bool keep = !(cz[j] > zup);
-#pragma unroll
-                for (int t = 0; t < kMaxCand; ++t)
-                    if (keep && t == m) {
-                        cf[t] = cf[j];
-                        cz[t] = cz[j];
-                    }
-                m += keep;
+        for (int i = 0; i < nE; ++i) {
+            // every later entry of the chunk lies behind every pixel of this warp: stop
+            if (sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
+            const float4 *row = reinterpret_cast<const float4 *>(&sE[i]);
+            const int4 bx = *reinterpret_cast<const int4 *>(row);
+            if (bx.w < rowLo || bx.y > rowHi || bx.z < colLo || bx.x > colHi) continue;  // warp-uniform
+            if (u < bx.x || u > bx.z || v < bx.y || v > bx.w) continue;
+            const float4 h = row[1];  // zLowSafe, mOut, flags, f
+            if (h.x > zup) continue;  // behind this pixel's covering face (and so is every later entry)
+            const int flags = __float_as_int(h.z);
+            float zlow = -kInf;
+            if (flags & kScreenValid) {
+                const float4 g0 = row[2], g1 = row[3];  // (x0, y0, a1, b1), (a2, b2, mIn, dRel)
+                float l0, l1, l2;
+                lambda_at(g0, g1.x, g1.y, px, py, l0, l1, l2);
+                if (l0 < -h.y || l1 < -h.y || l2 < -h.y) continue;  // certainly outside
+                const float zq = depth_at(row[4], l0, l1, l2);
+                if ((flags & kCertain) && l0 >= g1.z && l1 >= g1.z && l2 >= g1.z)
+                    zup = fminf(zup, zq * (1.0f + g1.w) + 2.0f);
+                zlow = h.x;
+                if (g1.w < 0.25f) zlow = fmaxf(zlow, zq * (1.0f - g1.w) - 2.0f);
+                if (zlow > zup) continue;  // certainly behind a covering face
             }
-            nCand = m;
-        }
-        if (nCand == kMaxCand) {
-            spill = true;
-            continue;
-        }
+            if (nCand == kMaxCand) {  // make room: drop candidates now known to lose
+                int m = 0;
 #pragma unroll
-        for (int t = 0; t < kMaxCand; ++t)
-            if (t == nCand) {
-                cf[t] = E.f;
-                cz[t] = zlow;
+                for (int j = 0; j < kMaxCand; ++j) {
+                    const bool keepC = !(cz[j] > zup);
+#pragma unroll
+                    for (int t = 0; t < kMaxCand; ++t)
+                        if (keepC && t == m) {
+                            cf[t] = cf[j];
+                            cz[t] = cz[j];
+                        }
+                    m += keepC;
+                }
+                nCand = m;
             }
-        ++nCand;
-    }
+            if (nCand == kMaxCand) {
+                spill = true;
+                continue;
+            }
+            const int fE = __float_as_int(h.w);
+#pragma unroll
+            for (int t = 0; t < kMaxCand; ++t)
+                if (t == nCand) {
+                    cf[t] = fE;
+                    cz[t] = zlow;
+                }
+            ++nCand;
+        }
     }  // chunks
 
     if (u >= dims.W || v >= dims.H) return;
