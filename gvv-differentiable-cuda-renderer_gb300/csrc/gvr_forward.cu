@@ -270,45 +270,69 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
         for (int tx = tx0; tx <= tx1; ++tx) atomicAdd(&cnt[ty * dims.tilesX + tx], 1);
 }
 
-// Exclusive scan of n counts by one 1024-thread block; start[n] = total.
 // Exclusive scan of count[0..n) into start[0..n], start[n] = total, by one
-// block of 1024 threads: each thread sums a contiguous run of ceil(n/1024)
-// counts, one block scan of the run sums, then each thread writes its run.
-// (Two passes over the counts and two barriers, instead of a block scan per
-// 1024 counts.)
+// block of 1024 threads, 8192 counts per pass: each thread loads 8
+// consecutive counts (two 16-byte loads when aligned), one block scan of
+// the per-thread sums, then each thread writes its 8 starts.
 __device__ __forceinline__ void scan_block(const int *__restrict__ count, int *__restrict__ start, int n) {
     __shared__ int warpSum[32];
+    __shared__ int carry;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int per = (n + 1023) / 1024;
-    const int lo = min(n, tid * per), hi = min(n, lo + per);
-    int sum = 0;
-    for (int i = lo; i < hi; ++i) sum += count[i];
-    int incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) warpSum[warp] = incl;
+    const bool vec = ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(start)) & 15) == 0;
+    if (tid == 0) carry = 0;
     __syncthreads();
-    if (warp == 0) {
-        const int w = warpSum[lane];
-        int wi = w;
+    for (int base = 0; base < n; base += 8192) {
+        const int i0 = base + 8 * tid;
+        int x[8];
+        if (vec && i0 + 8 <= n) {
+            const int4 a = *reinterpret_cast<const int4 *>(count + i0), c = *reinterpret_cast<const int4 *>(count + i0 + 4);
+            x[0] = a.x, x[1] = a.y, x[2] = a.z, x[3] = a.w, x[4] = c.x, x[5] = c.y, x[6] = c.z, x[7] = c.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) x[k] = i0 + k < n ? count[i0 + k] : 0;
+        }
+        int sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sum += x[k];
+        int incl = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += y;
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
         }
-        warpSum[lane] = wi - w;  // exclusive prefix of warp sums
+        if (lane == 31) warpSum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const int w = warpSum[lane];
+            int wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            warpSum[lane] = wi - w;  // exclusive prefix of warp sums
+        }
+        __syncthreads();
+        int run = carry + warpSum[warp] + incl - sum;
+        int st[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            st[k] = run;
+            run += x[k];
+        }
+        if (vec && i0 + 8 <= n) {
+            *reinterpret_cast<int4 *>(start + i0) = make_int4(st[0], st[1], st[2], st[3]);
+            *reinterpret_cast<int4 *>(start + i0 + 4) = make_int4(st[4], st[5], st[6], st[7]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (i0 + k < n) start[i0 + k] = st[k];
+        }
+        __syncthreads();  // every thread has read carry
+        if (tid == 1023) carry = run;
+        __syncthreads();
     }
-    __syncthreads();
-    int run = warpSum[warp] + incl - sum;
-    for (int i = lo; i < hi; ++i) {
-        const int x = count[i];
-        start[i] = run;
-        run += x;
-    }
-    if (tid == 1023) start[n] = run;
+    if (tid == 0) start[n] = carry;
 }
 
 __device__ __forceinline__ void bin_fill_item(const FwdJob &J, int i) {

@@ -258,12 +258,27 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         }
         if (tid <= kBuckets) sHist[tid] = 0;
 
-        for (int i = 0; i < nE; ++i) {
+        // The warp takes the sorted entries 32 at a time: one ballot marks
+        // those whose box meets the warp's 8x4 block, and only they are visited.
+        bool stop = false;
+        for (int base = 0; base < nE && !stop; base += 32) {
+            const int k = base + lane;
+            bool meets = false;
+            if (k < nE) {
+                const int4 bx = *reinterpret_cast<const int4 *>(&sE[k]);
+                meets = !(bx.w < rowLo || bx.y > rowHi || bx.z < colLo || bx.x > colHi);
+            }
+            unsigned todo = __ballot_sync(0xffffffffu, meets);
+            while (todo) {
+            const int i = base + __ffs(todo) - 1;
+            todo &= todo - 1;
             // every later entry of the chunk lies behind every pixel of this warp: stop
-            if (sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) break;
+            if (sBucketLo[i] > __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(zup)))) {
+                stop = true;
+                break;
+            }
             const float4 *row = reinterpret_cast<const float4 *>(&sE[i]);
             const int4 bx = *reinterpret_cast<const int4 *>(row);
-            if (bx.w < rowLo || bx.y > rowHi || bx.z < colLo || bx.x > colHi) continue;  // warp-uniform
             if (u < bx.x || u > bx.z || v < bx.y || v > bx.w) continue;
             const float4 h = row[1];  // zLowSafe, mOut, flags, f
             if (h.x > zup) continue;  // behind this pixel's covering face (and so is every later entry)
@@ -308,6 +323,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
                     cz[t] = zlow;
                 }
             ++nCand;
+            }  // entries of the group that meet the block
         }
     }  // chunks
 
