@@ -100,13 +100,15 @@ void fwd_carve_main(const GvrHandle *h, int B, int Ht, int Wt, const TileCfg &tc
     L.s.bigList = c.take<int>(BC * h->F);
 }
 
-// The counters cleared before every call (tile counts and cursors, big-list counts).
+// The counters cleared before every call (tile counts and cursors, big-list
+// counts, per-view depth ranges).
 void fwd_carve_counters(const GvrHandle *h, int B, const TileCfg &tc, Carver &c, FwdLayout &L) {
     if (h->attrs.compute_normal_map) return;
     const size_t BC = (size_t)B * h->attrs.num_cameras, T = (size_t)tc.tilesX(h) * tc.tilesY(h);
     L.s.tileCount = c.take<int>(BC * T);
     L.s.tileCursor = c.take<int>(BC * T);
     L.s.bigCount = c.take<int>(BC);
+    L.s.zRange = c.take<unsigned>(2 * BC);
 }
 
 FwdLayout fwd_layout(const GvrHandle *h, int B, int Ht, int Wt, void *base, const TileCfg &tc = TileCfg()) {

@@ -255,6 +255,26 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
     vf.s0 = make_float4(p0.x, p0.y, mOut, valid ? zmn * (10000.0f / 1.0025f) - 2.0f : -__int_as_float(0x7f800000));
     vf.s1 = s1;
     ws.vface[i] = vf;
+    // the view's range of finite, non-negative depth bounds (the raster's
+    // depth buckets span it): one pair of atomics per view per warp
+    {
+        const bool ranged = box.x <= box.z && box.y <= box.w && vf.s0.w >= 0.0f && vf.s0.w < __int_as_float(0x7f800000);
+        const unsigned bits = __float_as_uint(vf.s0.w);
+        const unsigned act = __activemask();
+        const int lane = threadIdx.x & 31;
+        unsigned pending = act;
+        while (pending) {  // the distinct views of the warp's items (two at most when F >= 32)
+            const int first = __ffs(pending) - 1;
+            const bool mine = __shfl_sync(act, bc, first) == bc;
+            const unsigned hiBits = __reduce_max_sync(act, mine && ranged ? bits : 0u);
+            const unsigned loInv = __reduce_max_sync(act, mine && ranged ? ~bits : 0u);
+            if (lane == first && hiBits) {
+                atomicMax(&ws.zRange[2 * bc], loInv);
+                atomicMax(&ws.zRange[2 * bc + 1], hiBits);
+            }
+            pending &= ~__ballot_sync(act, mine);
+        }
+    }
     if (box.x > box.z || box.y > box.w) return;
     const int sh = dims.tileShift, tH = dims.tileH;
     int tx0 = box.x >> sh, tx1 = box.z >> sh, ty0 = box.y / tH, ty1 = box.w / tH;

@@ -313,6 +313,8 @@ struct FwdScratch {
     int *bins;           // [kBigTiles*B*C*F]
     int *bigList;        // [B*C*F]
     int *bigCount;       // [B*C]
+    unsigned *zRange;    // [B*C*2] per view: max of ~bits(zLowSafe) (= ~min) and max of bits(zLowSafe)
+                         // over its faces with a finite, non-negative bound; 0 = none
     size_t zeroBytes;    // bytes from tileCount to clear per call (counts, cursors, big counts)
     void *zeroBase;
 };

@@ -30,7 +30,7 @@ namespace gvr {
 namespace {
 
 constexpr int kChunk = kTilePix;  // face entries staged per pass: one per thread
-constexpr int kBuckets = 64;      // depth buckets of the front-to-back order
+constexpr int kBuckets = 256;     // depth buckets of the front-to-back order
 constexpr int kMaxCand = 4;       // candidates a pixel keeps in registers
 
 // Face entry with its skip-test constants and its box clipped to the tile
@@ -152,7 +152,6 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     __shared__ Entry sE[kChunk];
     __shared__ float sBucketLo[kChunk];
     __shared__ int sHist[kBuckets + 1];
-    __shared__ unsigned sKeyLo, sKeyHi;
     const int T = dims.tilesX * dims.tilesY;
     const int tile = item % T, bc = item / T, b = bc / dims.C;
     const int tileW = dims.tileW, tileH = dims.tileH;
@@ -190,18 +189,19 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         cf[j] = -1;
         cz[j] = kInf;
     }
-    if (tid == 0) {
-        sKeyLo = 0x7f800000u;
-        sKeyHi = 0u;
-    }
-    if (tid <= kBuckets) sHist[tid] = 0;
+    // The view's range of finite, non-negative depth bounds, from the binning
+    // pass: every kept entry with such a bound lies in it.
+    const unsigned zr0 = ws.zRange[2 * bc], zr1 = ws.zRange[2 * bc + 1];
+    const float lo = zr1 ? __uint_as_float(~zr0) : kInf, hi = zr1 ? __uint_as_float(zr1) : 0.0f;
+    const float scale = hi > lo ? (float)kBuckets / (hi - lo) : 0.0f;
+    for (int k = tid; k <= kBuckets; k += kTilePix) sHist[k] = 0;
     for (int c0 = 0; c0 < nAll; c0 += kChunk) {
         // Each thread builds one entry of the chunk and keeps it in registers
         // until its place in the front-to-back order is known: a counting
-        // sort into kBuckets depth buckets spanning the chunk's finite depth
-        // lower bounds (faces without a bound go first).  sBucketLo[i] is a
-        // lower bound of the depth bound of entry i and of every entry after
-        // it, which is all the early exit needs.
+        // sort into kBuckets depth buckets spanning the view's depth bounds
+        // (faces without a bound go first).  sBucketLo[i] is a lower bound of
+        // the depth bound of entry i and of every entry after it, which is
+        // all the early exit needs.
         const int e = c0 + tid;
         bool keep = false;
         Entry E;
@@ -210,37 +210,34 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
             keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
         }
-        // finite, non-negative bounds order like unsigned ints
-        const bool ranged = keep && E.zLowSafe >= 0.0f && E.zLowSafe < kInf;
-        const unsigned kLo = __reduce_min_sync(0xffffffffu, ranged ? __float_as_uint(E.zLowSafe) : 0x7f800000u);
-        const unsigned kHi = __reduce_max_sync(0xffffffffu, ranged ? __float_as_uint(E.zLowSafe) : 0u);
-        __syncthreads();  // every warp is done walking the previous chunk; the sort state is reset
-        if (lane == 0) {
-            atomicMin(&sKeyLo, kLo);
-            atomicMax(&sKeyHi, kHi);
-        }
-        __syncthreads();
-        const float lo = __uint_as_float(sKeyLo), hi = __uint_as_float(sKeyHi);
-        const float scale = hi > lo ? (float)kBuckets / (hi - lo) : 0.0f;
         // 0: no usable bound; 1..kBuckets by depth
         const int q = !keep || !(E.zLowSafe >= lo) ? 0 : 1 + min(kBuckets - 1, (int)((E.zLowSafe - lo) * scale));
+        __syncthreads();  // every warp is done walking the previous chunk; the histogram is clear
         if (keep) atomicAdd(&sHist[q], 1);
         const int nE = __syncthreads_count(keep);
-        if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: 3 per lane, one warp scan
-            const int q0 = 3 * tid;
-            const int h0 = q0 <= kBuckets ? sHist[q0] : 0, h1 = q0 + 1 <= kBuckets ? sHist[q0 + 1] : 0,
-                      h2 = q0 + 2 <= kBuckets ? sHist[q0 + 2] : 0;
-            const int own = h0 + h1 + h2;
+        if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: kPer per lane, one warp scan
+            constexpr int kPer = (kBuckets + 1 + 31) / 32;
+            int h[kPer];
+            int own = 0;
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int qk = kPer * tid + k;
+                h[k] = qk <= kBuckets ? sHist[qk] : 0;
+                own += h[k];
+            }
             int incl = own;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, incl, o);
                 if (tid >= o) incl += y;
             }
-            const int ex = incl - own;
-            if (q0 <= kBuckets) sHist[q0] = ex;
-            if (q0 + 1 <= kBuckets) sHist[q0 + 1] = ex + h0;
-            if (q0 + 2 <= kBuckets) sHist[q0 + 2] = ex + h0 + h1;
+            int run = incl - own;
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int qk = kPer * tid + k;
+                if (qk <= kBuckets) sHist[qk] = run;
+                run += h[k];
+            }
         }
         __syncthreads();
         if (keep) {
@@ -251,12 +248,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             sBucketLo[pos] = q == 0 ? -kInf : q == 1 ? lo : lo + (float)(q - 1) * (0.999f / scale);
         }
         __syncthreads();
-        // the sort state is free until the next chunk's first barrier
-        if (tid == 0) {
-            sKeyLo = 0x7f800000u;
-            sKeyHi = 0u;
-        }
-        if (tid <= kBuckets) sHist[tid] = 0;
+        for (int k = tid; k <= kBuckets; k += kTilePix) sHist[k] = 0;  // free until the next chunk's first barrier
 
         // The warp takes the sorted entries 32 at a time: one ballot marks
         // those whose box meets the warp's 8x4 block, and only they are visited.

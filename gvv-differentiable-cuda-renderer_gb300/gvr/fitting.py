@@ -167,36 +167,55 @@ class Fitter:
     # Adam step sizes per parameter group (coefficient units, rad / mm, SH)
     LR = {"shape": 0.05, "albedo": 0.05, "rot": 0.01, "trans": 2.0, "sh": 0.01}
 
-    def __init__(self, model: MorphableModel, num_views=4, size=512, albedo_position=True):
+    def __init__(self, model: MorphableModel, num_views=4, size=512, albedo_position=True, model_to_data=False,
+                 image_filter_size=1):
         """albedo_position: the renderer's backward also moves vertices by
         the change of their interpolated colour (GVR_BACKWARD_ALBEDO_POSITION);
         without it the position gradient is the reference's, which leaves
         that term out and so is not the loss's derivative for per-vertex
-        colours."""
+        colours.
+
+        model_to_data: the fit's residual compares the render with the
+        target as the renderer passes it through (target_image_out), so the
+        residual's gradient also reaches the vertices through the target
+        image's own gradient at each covered pixel, estimated over an
+        image_filter_size window (the reference's model-to-data term,
+        CUDABasedRasterizationGrad.cu:531-555): a surface point is pulled
+        toward where the target looks like its render, which moves
+        silhouettes that the shading gradient alone cannot."""
         self.model = model
         self.C, self.size = num_views, size
         self.backward_flags = _lib.BACKWARD_ALBEDO_POSITION if albedo_position else 0
+        self.model_to_data = model_to_data
         dev = model.device
         self.handle = renderer.get_handle(model.faces, model.uvs, model.N, num_views, size, size, "vertexColor",
-                                          "shaded", device=dev)
+                                          "shaded", image_filter_size=image_filter_size, device=dev)
         extr, intr = fit_cameras(num_views, size)
         self.extr = torch.from_numpy(extr).to(dev)
         self.intr = torch.from_numpy(intr).to(dev)
         self._tex = torch.zeros((1, 1, 1, 3), device=dev)
 
-    def render(self, params, with_face=False):
-        """[B, C, H, W, 3] renders of a [B, 193] parameter tensor (differentiable)."""
+    def render(self, params, with_face=False, target=None):
+        """[B, C, H, W, 3] renders of a [B, 193] parameter tensor
+        (differentiable), then the face ids if `with_face`, then, if a
+        `target` [B, C, H, W, 3] is given, the target as passed through the
+        renderer (equal to it; its gradient reaches the vertices through the
+        model-to-data term)."""
         B = params.shape[0]
         dev = self.model.device
         V = self.model.vertices(params)
         col = self.model.colors(params)
         sh = params[:, PARAM_SLICES["sh"]].unsqueeze(1).expand(B, self.C, N_SH).contiguous()
-        tgt = torch.zeros((B, self.C, self.size, self.size, 3), device=dev)
-        bary, face, img, vn, _, _ = renderer.RenderFunction.apply(
+        if target is None:
+            tgt = torch.zeros((B, self.C, self.size, self.size, 3), device=dev)
+        else:
+            tgt = target.expand(B, self.C, self.size, self.size, 3).contiguous()
+        bary, face, img, vn, tout, _ = renderer.RenderFunction.apply(
             self.handle, V.contiguous(), col.contiguous(), self._tex.expand(B, 1, 1, 3).contiguous(), sh, tgt,
             self.extr.expand(B, self.C, 12).contiguous(), self.intr.expand(B, self.C, 9).contiguous(),
             self.backward_flags)
-        return (img, face) if with_face else img
+        out = (img,) + ((face,) if with_face else ()) + ((tout,) if target is not None else ())
+        return out if len(out) > 1 else img
 
     @staticmethod
     def loss(img, target):
@@ -210,7 +229,9 @@ class Fitter:
         foreground in both the render and the target, one pixel in from
         either silhouette: shading cannot reduce the residual of a pixel
         that only one image covers, and the renderer's gradient is not the
-        derivative on the flipped-normal pixels at the silhouette; "all"
+        derivative on the flipped-normal pixels at the silhouette;
+        "rendered" uses every pixel the render covers (with model_to_data,
+        those the target does not cover pull the silhouette in); "all"
         uses every pixel.  The RMSE recorded (and compared with `goal`) is
         always over every pixel.  Records every element's RMSE per step and
         the GPU time (CUDA events, read back once at the end) to the first
@@ -237,18 +258,22 @@ class Fitter:
         target_fg = (target - bg).abs().amax(-1) > 0        # the background is exactly (0, 1, 0)
         events[0].record()
         for k in range(steps + 1):
-            img, face = self.render(p, with_face=True)
+            if self.model_to_data:
+                img, face, ref = self.render(p, with_face=True, target=target)
+            else:
+                img, face = self.render(p, with_face=True)
+                ref = target
             per = self.loss(img, target)
             rmse = torch.sqrt(per.detach())
             hist[k] = rmse
             events[k + 1].record()
             if k == steps:
                 break
-            if objective == "interior":
-                keep = interior_mask((face >= 0) & target_fg)
-                obj = (((img - target) ** 2) * keep[..., None]).flatten(1).sum(1) / img[0].numel()
+            if objective in ("interior", "rendered"):
+                keep = interior_mask((face >= 0) & target_fg) if objective == "interior" else (face >= 0).float()
+                obj = (((img - ref) ** 2) * keep[..., None]).flatten(1).sum(1) / img[0].numel()
             else:
-                obj = per
+                obj = self.loss(img, ref)
             g, = torch.autograd.grad(obj.sum(), p)
             if fallback is not None and k == fallback[0]:
                 bad = rmse > fallback[1]
