@@ -11,7 +11,10 @@ Workload (one step = one forward and one backward over one batch):
 One JSON line on rank 0.  `value` is device time with inputs resident in
 HBM (L2 flushed between steps by a 256 MiB memset outside the timed events);
 `e2e` goes through the C ABI with pinned host buffers and the host<->device
-copies inside the timed region.  Under torchrun every rank renders its own
+copies inside the timed region: every step copies its inputs in and its
+render and gradients out, on copy streams that overlap the kernels of the
+neighbouring steps (the serial form, one stream, is reported beside it).
+Under torchrun every rank renders its own
 replica (the path needs no cross-GPU exchange), `value` is the total pixels
 of all ranks / the slowest rank's time.
 """
@@ -325,31 +328,97 @@ def run_gvr(args):
                 "bytes_per_launch": kb, "avg_launch_ms": dom_avg, "peak_source": peak_src}
     step_bytes = algorithmic_bytes(P, C, N, F, Ht, Wt, int(textured), int(s["albedo_mode"] == "vertexColor"))
 
-    # ---- end to end through the C ABI with host buffers
-    hres = {k: torch.empty(out[k].shape, dtype=out[k].dtype).pin_memory() for k in ("render", "gpos", "gtex", "gsh")}
+    # ---- end to end through the C ABI with host buffers.  Every step copies
+    # its inputs in from pinned host memory and its render and gradients out.
+    # Pipelined: two buffer sets; inputs go in on one copy stream, results
+    # out on another, the forward and backward run on the compute stream, so
+    # step i's copies overlap the kernels of steps i-1 and i+1 (and the
+    # upstream gradient's copy overlaps the step's own forward).  The serial
+    # form (copy in, compute, copy out on one stream) is reported beside it.
+    hres = [{k: torch.empty(out[k].shape, dtype=out[k].dtype).pin_memory() for k in ("render", "gpos", "gtex", "gsh")}
+            for _ in range(2)]
     h2d = sum(v.numel() * v.element_size() for v in host.values())
-    d2h = sum(v.numel() * v.element_size() for v in hres.values())
+    d2h = sum(v.numel() * v.element_size() for v in hres[0].values())
+    small = [k for k in host if k != "grad_render"]
+    dsets = [d, {k: torch.empty_like(v) for k, v in d.items()}]
+    osets = [out, {k: torch.empty_like(v) for k, v in out.items()}]
+    fas, bas = [], []
+    for dd, oo in zip(dsets, osets):
+        fas.append(_lib.GvrForwardArgs(B, Ht, Wt, p(dd["vertex_pos"]), p(dd["vertex_color"]), p(dd["texture"]),
+                                       p(dd["sh_coeff"]), None, p(dd["extrinsics"]), p(dd["intrinsics"]), p(oo["bary"]),
+                                       p(oo["face"]), p(oo["render"]), p(oo["vnorm"]), None, None, p(fws), fws.numel()))
+        bas.append(_lib.GvrBackwardArgs(B, Ht, Wt, p(dd["grad_render"]), p(dd["vertex_pos"]), p(dd["vertex_color"]),
+                                        p(dd["texture"]), p(dd["sh_coeff"]), None, p(oo["vnorm"]), None, p(oo["face"]),
+                                        None, p(dd["extrinsics"]), p(dd["intrinsics"]), p(oo["gpos"]), p(oo["gcol"]),
+                                        p(oo["gtex"]), p(oo["gsh"]), p(bws), bws.numel()))
+    s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ev = lambda: torch.cuda.Event()
+    comp_done, out_done = [ev(), ev()], [ev(), ev()]
+    for e_ in comp_done + out_done:
+        e_.record(stream)
 
-    def e2e_step():
+    def e2e_pipelined(i):
+        j = i & 1
+        dd, oo, hh = dsets[j], osets[j], hres[j]
+        in_small, in_grad, fwd_done = ev(), ev(), ev()
+        s_in.wait_event(comp_done[j])              # step i-2's kernels are done with these inputs
+        with torch.cuda.stream(s_in):
+            for k in small:
+                dd[k].copy_(host[k], non_blocking=True)
+            in_small.record(s_in)
+            dd["grad_render"].copy_(host["grad_render"], non_blocking=True)
+            in_grad.record(s_in)
+        stream.wait_event(in_small)
+        stream.wait_event(out_done[j])             # step i-2's results are copied out of these outputs
+        _lib.check(L.gvr_forward(h.ptr, ctypes.byref(fas[j]), sp))
+        fwd_done.record(stream)
+        stream.wait_event(in_grad)
+        _lib.check(L.gvr_backward(h.ptr, ctypes.byref(bas[j]), sp))
+        comp_done[j].record(stream)
+        s_out.wait_event(fwd_done)
+        with torch.cuda.stream(s_out):
+            hh["render"].copy_(oo["render"], non_blocking=True)
+            s_out.wait_event(comp_done[j])
+            for k in ("gpos", "gtex", "gsh"):
+                hh[k].copy_(oo[k], non_blocking=True)
+            out_done[j].record(s_out)
+
+    def e2e_serial():
         for k, v in host.items():
             d[k].copy_(v, non_blocking=True)
         step()
-        for k, v in hres.items():
+        for k, v in hres[0].items():
             v.copy_(out[k], non_blocking=True)
 
-    e2e_ms = float("nan")
+    e2e_ms = e2e_serial_ms = float("nan")
     if not args.no_e2e:
-        for _ in range(max(1, args.warmup)):
-            e2e_step()
+        torch.cuda.synchronize()
+        for i in range(max(2, args.warmup)):
+            e2e_pipelined(i)
         torch.cuda.synchronize()
         barrier(world)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
-            e2e_step()
+        s_in.wait_event(e0)
+        for i in range(args.steps):
+            e2e_pipelined(i)
+        stream.wait_stream(s_out)
         e1.record(stream)
         torch.cuda.synchronize()
         e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world)
+        # every step's results reached the host: the last two buffer sets match a serial step
+        for k in ("render", "gtex"):
+            if not torch.equal(hres[(args.steps - 1) & 1][k], osets[(args.steps - 1) & 1][k].cpu()):
+                raise RuntimeError(f"pipelined e2e: host copy of {k} differs from the device result")
+        for _ in range(max(1, args.warmup)):
+            e2e_serial()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_serial()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_serial_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world)
         barrier(world)
 
     if rank != 0:
@@ -372,7 +441,10 @@ def run_gvr(args):
             "roofline": roofline,
             "kernels_ms_per_step": {k: round(v[1] / args.steps, 5) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
             "e2e": {"value": world * P / (e2e_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": e2e_ms,
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "pipeline": "2 buffer sets; copies in and out on their own streams overlap the kernels",
+                    "serial_ms_per_step": e2e_serial_ms,
+                    "serial_value": world * P / (e2e_serial_ms / 1e3) / 1e6},
             "gpu_launches": launches, "timed_wall_s": t_wall,
             "clocks": clk, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)

@@ -78,6 +78,19 @@ __device__ __forceinline__ void reduce_scatter_step(float (&r)[32], int lane) {
     }
 }
 
+// Adds (g0, g1, g2) to a texel's three floats with one 8-byte vector
+// atomic and one scalar one: of two consecutive floats one starts on an
+// 8-byte boundary.
+__device__ __forceinline__ void add_texel(float *t, float g0, float g1, float g2) {
+    if ((reinterpret_cast<uintptr_t>(t) & 7) == 0) {
+        atomicAdd(reinterpret_cast<float2 *>(t), make_float2(g0, g1));
+        atomicAdd(t + 2, g2);
+    } else {
+        atomicAdd(t, g0);
+        atomicAdd(reinterpret_cast<float2 *>(t + 1), make_float2(g1, g2));
+    }
+}
+
 struct BwdIO {
     const float *grad_render;  // [B,C,H,W,3]
     const float *verts;        // [B,N,3]
@@ -187,12 +200,9 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
 #pragma unroll
                 for (int ch = 0; ch < 3; ++ch)
                     alb[ch] = wv0 * (wu0 * cLL[ch] + wu1 * cHL[ch]) + wv1 * (wu0 * cLH[ch] + wu1 * cHH[ch]);
-                if (!flipped) {
-                    float *tg = io.tex_grad + (((size_t)b * dims.Ht + iv) * dims.Wt + iu) * 3;
-                    atomicAdd(tg + 0, G[0] * JCoAl[0]);
-                    atomicAdd(tg + 1, G[1] * JCoAl[1]);
-                    atomicAdd(tg + 2, G[2] * JCoAl[2]);
-                }
+                if (!flipped)
+                    add_texel(io.tex_grad + (((size_t)b * dims.Ht + iv) * dims.Wt + iu) * 3, G[0] * JCoAl[0],
+                              G[1] * JCoAl[1], G[2] * JCoAl[2]);
             }
             if (MODE == GVR_ALBEDO_TEXTURED_BILINEAR) {  // the lookup and its derivative: four texels
                 const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
@@ -204,10 +214,9 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
 #pragma unroll
-                    for (int ch = 0; ch < 3; ++ch) {
-                        alb[ch] += w[k] * tex[3 * (size_t)idx[k] + ch];
-                        atomicAdd(tgb + 3 * (size_t)idx[k] + ch, w[k] * (G[ch] * JCoAl[ch]));
-                    }
+                    for (int ch = 0; ch < 3; ++ch) alb[ch] += w[k] * tex[3 * (size_t)idx[k] + ch];
+                    add_texel(tgb + 3 * (size_t)idx[k], w[k] * (G[0] * JCoAl[0]), w[k] * (G[1] * JCoAl[1]),
+                              w[k] * (G[2] * JCoAl[2]));
                 }
             }
             // Pv: per-pixel vector applied with the stored barycentrics (target term);

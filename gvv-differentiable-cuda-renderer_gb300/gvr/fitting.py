@@ -168,7 +168,7 @@ class Fitter:
     LR = {"shape": 0.05, "albedo": 0.05, "rot": 0.01, "trans": 2.0, "sh": 0.01}
 
     def __init__(self, model: MorphableModel, num_views=4, size=512, albedo_position=True, model_to_data=False,
-                 image_filter_size=1):
+                 image_filter_size=1, silhouette=0.0, contour_radius=48):
         """albedo_position: the renderer's backward also moves vertices by
         the change of their interpolated colour (GVR_BACKWARD_ALBEDO_POSITION);
         without it the position gradient is the reference's, which leaves
@@ -182,11 +182,24 @@ class Fitter:
         image_filter_size window (the reference's model-to-data term,
         CUDABasedRasterizationGrad.cu:531-555): a surface point is pulled
         toward where the target looks like its render, which moves
-        silhouettes that the shading gradient alone cannot."""
+        silhouettes that the shading gradient alone cannot.
+
+        silhouette > 0: adds silhouette * sum over the render's silhouette
+        pixels of the distance (pixels, up to contour_radius) from the
+        target's silhouette, per pixel of the image.  The distance field is
+        handed to the renderer as its target image, so the same
+        model-to-data term turns the field's gradient at each silhouette
+        pixel into a vertex gradient: the render's outline is pulled onto
+        the target's, from inside and outside (the photometric gradient has
+        no visibility term and cannot move an outline)."""
         self.model = model
         self.C, self.size = num_views, size
         self.backward_flags = _lib.BACKWARD_ALBEDO_POSITION if albedo_position else 0
         self.model_to_data = model_to_data
+        self.silhouette = float(silhouette)
+        self.contour_radius = int(contour_radius)
+        if model_to_data and silhouette > 0:
+            raise ValueError("model_to_data and silhouette both use the renderer's target image")
         dev = model.device
         self.handle = renderer.get_handle(model.faces, model.uvs, model.N, num_views, size, size, "vertexColor",
                                           "shaded", image_filter_size=image_filter_size, device=dev)
@@ -222,7 +235,8 @@ class Fitter:
         """Photometric L2: mean squared error over every pixel and channel, per batch element."""
         return ((img - target) ** 2).flatten(1).mean(1)
 
-    def fit(self, target, init, steps=200, goal=0.01, fallback=None, lr=None, decay=0.05, objective="interior"):
+    def fit(self, target, init, steps=200, goal=0.01, fallback=None, lr=None, decay=0.05, objective="interior",
+            betas=(0.9, 0.999)):
         """Adam on the photometric L2 loss from `init` [B, 193], step sizes
         decaying geometrically to `decay` times their start over `steps`.
         objective="interior" descends the loss over the pixels that are
@@ -250,16 +264,22 @@ class Fitter:
         # Adam with per-coordinate step sizes (bias-corrected moments)
         m = torch.zeros_like(p)
         v = torch.zeros_like(p)
-        b1, b2, eps = 0.9, 0.999, 1e-8
+        (b1, b2), eps = betas, 1e-8
         t_count = torch.zeros(B, 1, device=dev)
         hist = torch.empty((steps + 1, B), device=dev)
         events = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 2)]
         bg = torch.tensor([0.0, 1.0, 0.0], device=dev)
         target_fg = (target - bg).abs().amax(-1) > 0        # the background is exactly (0, 1, 0)
         events[0].record()
+        if self.silhouette > 0:
+            field = torch.zeros_like(target)
+            field[..., 0] = contour_distance(target_fg, self.contour_radius)
         for k in range(steps + 1):
             if self.model_to_data:
                 img, face, ref = self.render(p, with_face=True, target=target)
+            elif self.silhouette > 0:
+                img, face, dist = self.render(p, with_face=True, target=field)
+                ref = target
             else:
                 img, face = self.render(p, with_face=True)
                 ref = target
@@ -274,6 +294,9 @@ class Fitter:
                 obj = (((img - ref) ** 2) * keep[..., None]).flatten(1).sum(1) / img[0].numel()
             else:
                 obj = self.loss(img, ref)
+            if self.silhouette > 0:
+                edge = silhouette_pixels(face >= 0)
+                obj = obj + self.silhouette * (dist[..., 0] * edge).flatten(1).sum(1) / img[0].numel()
             g, = torch.autograd.grad(obj.sum(), p)
             if fallback is not None and k == fallback[0]:
                 bad = rmse > fallback[1]
@@ -309,6 +332,29 @@ def interior_mask(fg):
     outside = (~fg).float().view(B * C, 1, H, W)
     grown = torch.nn.functional.max_pool2d(outside, 3, stride=1, padding=1)
     return (1.0 - grown).view(B, C, H, W)
+
+
+def contour_distance(fg, radius):
+    """[B, C, H, W] bool -> float: for each pixel the chessboard distance
+    (pixels, capped at `radius`) to the nearest pixel of the other side of
+    the outline, minus one: 0 on the pixels either side of it.  Computed by
+    `radius` 3x3 dilations of each side."""
+    B, C, H, W = fg.shape
+    out = torch.zeros((B * C, 1, H, W), device=fg.device)
+    for side in (fg, ~fg):
+        x = side.float().view(B * C, 1, H, W)
+        for _ in range(radius):
+            out += 1.0 - x
+            x = torch.nn.functional.max_pool2d(x, 3, stride=1, padding=1)
+    return (out - 1.0).clamp_(min=0.0).view(B, C, H, W)
+
+
+def silhouette_pixels(fg):
+    """[B, C, H, W] bool -> float mask of the foreground pixels with a
+    background pixel among their 8 neighbours."""
+    B, C, H, W = fg.shape
+    bgn = torch.nn.functional.max_pool2d((~fg).float().view(B * C, 1, H, W), 3, stride=1, padding=1)
+    return (fg.float().view(B * C, 1, H, W) * bgn).view(B, C, H, W)
 
 
 def make_targets(fitter: Fitter, rng, batch=1):
