@@ -66,7 +66,10 @@ def parse():
 
 
 def algorithmic_bytes(P, C, N, F, Ht, Wt, textured, vertex_color):
-    """Bytes one fwd+bwd call must move ('Algorithmic bytes')."""
+    """Bytes one fwd+bwd call must move: per pixel the render, face id,
+    barycentrics, upstream gradient and their reads (64 B); per view the
+    vertex normals, face records and (textured) UVs; the texture and its
+    gradient; vertex positions and their gradient; SH and its gradient."""
     return (P * 64 + C * (12 * N + 12 * F + 24 * F * textured + 12 * N) + 12 * N * vertex_color +
             24 * Ht * Wt * textured + 24 * N + 216 * C)
 
@@ -559,14 +562,15 @@ def run_fit_bench(args):
     from gvr import fitting, native_build, proposal, tc
     native_build.build()
     model = fitting.MorphableModel(num_vertices=28000, seed=0, device=dev)
-    fitter = fitting.Fitter(model, num_views=4, size=512)
+    fitter = fitting.Fitter(model, num_views=4, size=512, silhouette=fitting.Fitter.SILHOUETTE)
     seeds = list(range(1_000_000, 1_000_000 + args.fits))
     line = {"n_gpus": world, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic", "unit": "ms"}
     plain = proposal.evaluate(fitter, None, seeds, batch=args.fit_batch)
     ps = _fit_summary(plain, args.fit_batch)
     cfg = {"workload": "morphable-model fit: 28,000 V displaced-sphere mean + 80 shape + 80 albedo smooth bases, "
-                       "pose 6, SH 27; 4 views at 512^2; 200 Adam steps on photometric L2; goal RMSE <= 0.01",
+                       "pose 6, SH 27; 4 views at 512^2; 200 Adam steps on photometric L2 + silhouette term "
+                       "(distance field to the target outline through the model-to-data gradient); goal RMSE <= 0.01",
            "fits": args.fits, "fit_batch": args.fit_batch}
     if args.workload == "fit":
         line.update(metric="fit GPU ms to RMSE<=0.01 (plain, per fit)", value=ps["mean_gpu_ms_to_solution_per_fit"],

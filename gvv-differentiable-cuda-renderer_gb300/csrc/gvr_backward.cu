@@ -127,8 +127,18 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
     const size_t p = ((size_t)bc * dims.H + v) * dims.W + u;
     const int F = topo.F, N = topo.N;
 
+    // the view's camera and SH coefficients, read by every pixel: staged
+    // once per block (uniform global loads per pixel crowd the LSU pipe)
+    __shared__ Camera sCam;
+    __shared__ float sSH[27];
+    {
+        constexpr int kCamWords = (int)(sizeof(Camera) / sizeof(float));
+        if (tid < kCamWords) reinterpret_cast<float *>(&sCam)[tid] = reinterpret_cast<const float *>(ws.cams + bc)[tid];
+        else if (tid < kCamWords + 27) sSH[tid - kCamWords] = io.sh[(size_t)bc * 27 + (tid - kCamWords)];
+    }
     int f = inImage ? io.face[p] : -1;
     if (f >= F) f = -1;  // ids outside [0, F) carry no face
+    __syncthreads();
     float val[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) val[k] = 0.0f;
@@ -137,7 +147,7 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
     for (int k = 0; k < (SHADED ? 32 : 1); ++k) shv[k] = 0.0f;
 
     if (f >= 0) {
-        const Camera &cam = ws.cams[bc];
+        const Camera &cam = sCam;
         const V3 origS = v3(cam.origS[0], cam.origS[1], cam.origS[2]);
         const V3 d = pixel_ray(cam, u, v);
         const FaceSetup fs = load_face(&ws.geo[(size_t)b * F + f]);
@@ -162,7 +172,7 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
             if (flipped) n = v3(-n.x, -n.y, -n.z);
             const float *gr = io.grad_render + 3 * p;
             const float G[3] = {gr[0], gr[1], gr[2]};
-            const float *sh = io.sh + (size_t)bc * 27;
+            const float *sh = sSH;
             float basis[9];
             sh_basis(n, basis);
             float JCoAl[3] = {1.0f, 1.0f, 1.0f};
