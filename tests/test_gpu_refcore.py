@@ -50,6 +50,30 @@ def compare_visibility(s, ours, ref, tag=""):
     return orc, int(tie.sum())
 
 
+def _time_ours(s, reps=20):
+    """Mean ms of one render_forward + render_backward call pair on the
+    scene (CUDA events around `reps` calls after 3 warm-up calls)."""
+    import torch
+    from gvr import renderer
+    from test_gpu_parity import _handle, _tensors
+    h, t = _handle(s, None, None, 1), _tensors(s)
+
+    def once():
+        bary, face, img, vn, _, _ = renderer.render_forward(h, t["vertex_pos"], t["vertex_color"], t["texture"],
+                                                            t["sh_coeff"], t["extrinsics"], t["intrinsics"])
+        renderer.render_backward(h, t["grad_render"], t["vertex_pos"], t["vertex_color"], t["texture"], t["sh_coeff"],
+                                 t["target_image"], vn, bary, face, None, t["extrinsics"], t["intrinsics"], 0)
+    for _ in range(3):
+        once()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        once()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 MODES = [("vertexColor", "shaded"), ("textured", "shaded"), ("textured", "shadeless"), ("normal", "shaded"),
          ("lighting", "shadeless"), ("foregroundMask", "shaded")]
 
@@ -73,7 +97,8 @@ def test_workloads_match_reference_kernels(ref_nofma, ref_default):
         g = ref_default.backward(s, d)
         print(f"\n{s['num_views']}x{s['width']}^2, F={s['faces'].shape[0]}: tie pixels {ties}, "
               f"default-build (FMA) face mismatch rate {mism:.2e}, reference kernels: forward "
-              f"{d['ms']:.2f} ms, backward {g['ms']:.2f} ms (default build), forward {ref['ms']:.2f} ms (-fmad=false)")
+              f"{d['ms']:.2f} ms, backward {g['ms']:.2f} ms (default build), forward {ref['ms']:.2f} ms (-fmad=false); "
+              f"this build through renderer.render_forward/backward: {_time_ours(s):.3f} ms fwd+bwd")
         assert mism < 0.01
 
 
