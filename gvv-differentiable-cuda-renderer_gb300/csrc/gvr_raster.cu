@@ -97,18 +97,27 @@ __device__ __forceinline__ float entry_depth(const Entry &E, float l0, float l1,
     return depth_at(make_float4(E.r0, E.r1, E.r2, 0.0f), l0, l1, l2);
 }
 
-// False when no pixel centre of the entry's clipped box can pass the
-// "not certainly outside" test: each screen barycentric is affine, so its
-// maximum over the box is at the corner picked by the signs of its slopes.
+// False when no pixel centre of the box [x0, x1] x [y0, y1] can pass the
+// "not certainly outside" test of a screen-valid entry: each screen
+// barycentric is affine, so its maximum over the box is at the corner
+// picked by the signs of its slopes.  (The margin mOut leaves slack far
+// above FP32 rounding, so a corner and a pixel evaluated with different
+// rounding cannot disagree on a face the exact test could accept.)
+__device__ __forceinline__ bool may_cover_box(const float4 &g0, float a2, float b2, float mOut, int x0, int x1, int y0,
+                                              int y1) {
+    const float xl = x0 + 0.5f, xh = x1 + 0.5f, yl = y0 + 0.5f, yh = y1 + 0.5f;
+    const float a0 = -(g0.z + a2), b0 = -(g0.w + b2);
+    float l0, l1, l2, s, t;
+    lambda_at(g0, a2, b2, a0 >= 0.0f ? xh : xl, b0 >= 0.0f ? yh : yl, l0, s, t);
+    lambda_at(g0, a2, b2, g0.z >= 0.0f ? xh : xl, g0.w >= 0.0f ? yh : yl, s, l1, t);
+    lambda_at(g0, a2, b2, a2 >= 0.0f ? xh : xl, b2 >= 0.0f ? yh : yl, s, t, l2);
+    return !(l0 < -mOut || l1 < -mOut || l2 < -mOut);
+}
+
+// The same test over the entry's whole clipped box.
 __device__ __forceinline__ bool may_cover_rect(const Entry &E) {
     if (!(E.flags & kScreenValid)) return true;
-    const float xl = E.bx0 + 0.5f, xh = E.bx1 + 0.5f, yl = E.by0 + 0.5f, yh = E.by1 + 0.5f;
-    const float a0 = -(E.a1 + E.a2), b0 = -(E.b1 + E.b2);
-    float l0, l1, l2, s, t;
-    entry_lambda(E, a0 >= 0.0f ? xh : xl, b0 >= 0.0f ? yh : yl, l0, s, t);
-    entry_lambda(E, E.a1 >= 0.0f ? xh : xl, E.b1 >= 0.0f ? yh : yl, s, l1, t);
-    entry_lambda(E, E.a2 >= 0.0f ? xh : xl, E.b2 >= 0.0f ? yh : yl, s, t, l2);
-    return !(l0 < -E.mOut || l1 < -E.mOut || l2 < -E.mOut);
+    return may_cover_box(make_float4(E.x0, E.y0, E.a1, E.b1), E.a2, E.b2, E.mOut, E.bx0, E.bx1, E.by0, E.by1);
 }
 
 // May the face win the pixel against the certain depth bound zup?
@@ -250,15 +259,26 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         __syncthreads();
         for (int k = tid; k <= kBuckets; k += kTilePix) sHist[k] = 0;  // free until the next chunk's first barrier
 
-        // The warp takes the sorted entries 32 at a time: one ballot marks
-        // those whose box meets the warp's 8x4 block, and only they are visited.
+        // The warp takes the sorted entries 32 at a time, one per lane: a
+        // ballot marks those whose triangle may cover a pixel centre of the
+        // warp's 8x4 block (box overlap, then the corner test over the part
+        // of the box inside the block), and only they are visited.
         bool stop = false;
         for (int base = 0; base < nE && !stop; base += 32) {
             const int k = base + lane;
             bool meets = false;
             if (k < nE) {
-                const int4 bx = *reinterpret_cast<const int4 *>(&sE[k]);
-                meets = !(bx.w < rowLo || bx.y > rowHi || bx.z < colLo || bx.x > colHi);
+                const float4 *rk = reinterpret_cast<const float4 *>(&sE[k]);
+                const int4 bx = *reinterpret_cast<const int4 *>(rk);
+                const int xl = max(bx.x, colLo), xh = min(bx.z, colHi), yl = max(bx.y, rowLo), yh = min(bx.w, rowHi);
+                meets = xl <= xh && yl <= yh;
+                if (meets) {
+                    const float4 hk = rk[1];  // zLowSafe, mOut, flags, f
+                    if (__float_as_int(hk.z) & kScreenValid) {
+                        const float4 g1 = rk[3];
+                        meets = may_cover_box(rk[2], g1.x, g1.y, hk.y, xl, xh, yl, yh);
+                    }
+                }
             }
             unsigned todo = __ballot_sync(0xffffffffu, meets);
             while (todo) {
