@@ -166,9 +166,10 @@ class Fitter:
 
     # Adam step sizes per parameter group (coefficient units, rad / mm, SH),
     # tuned with the silhouette term on 4 views at 512^2 (median final RMSE
-    # over 16 draws from the mean: 0.017 with these, 0.041 with half the
-    # shape / pose and a third of the albedo / SH step sizes)
-    LR = {"shape": 0.1, "albedo": 0.15, "rot": 0.02, "trans": 4.0, "sh": 0.03}
+    # over 16 draws from the mean: 0.015 with these, 0.018 with half of
+    # them, 0.041 with a quarter of the shape / pose and a sixth of the
+    # albedo / SH step sizes and the uncentred outline field)
+    LR = {"shape": 0.2, "albedo": 0.3, "rot": 0.04, "trans": 8.0, "sh": 0.06}
     SILHOUETTE = 0.03   # weight of the silhouette term in the tuned setting
 
     def __init__(self, model: MorphableModel, num_views=4, size=512, albedo_position=True, model_to_data=False,
