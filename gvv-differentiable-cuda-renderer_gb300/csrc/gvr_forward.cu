@@ -285,9 +285,16 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
         ws.bigList[(size_t)bc * F + k] = f;
         return;
     }
-    int *cnt = ws.tileCount + (size_t)bc * T;
-    for (int ty = ty0; ty <= ty1; ++ty)
-        for (int tx = tx0; tx <= tx1; ++tx) atomicAdd(&cnt[ty * dims.tilesX + tx], 1);
+    // One atomic per distinct tile of the warp per round: the lanes of a warp
+    // hold neighbouring faces, which share most of their tiles.
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, w = tx1 - tx0 + 1;
+    const int rounds = __reduce_max_sync(act, nt);
+    for (int r = 0; r < rounds; ++r) {
+        const long long key = r < nt ? (long long)bc * T + (ty0 + r / w) * dims.tilesX + tx0 + r % w : -1ll;
+        const unsigned peers = __match_any_sync(act, key);
+        if (key >= 0 && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&ws.tileCount[key], __popc(peers));
+    }
 }
 
 // Exclusive scan of count[0..n) into start[0..n], start[n] = total, by one
@@ -364,14 +371,23 @@ __device__ __forceinline__ void bin_fill_item(const FwdJob &J, int i) {
     if (box.x > box.z || box.y > box.w) return;
     const int sh = dims.tileShift, tH = dims.tileH;
     int tx0 = box.x >> sh, tx1 = box.z >> sh, ty0 = box.y / tH, ty1 = box.w / tH;
-    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > dims.bigTiles) return;
+    const int w = tx1 - tx0 + 1, nt = w * (ty1 - ty0 + 1);
+    if (nt > dims.bigTiles) return;
     const int T = dims.tilesX * dims.tilesY;
-    for (int ty = ty0; ty <= ty1; ++ty)
-        for (int tx = tx0; tx <= tx1; ++tx) {
-            size_t t = (size_t)bc * T + ty * dims.tilesX + tx;
-            int pos = atomicAdd(&ws.tileCursor[t], 1);
-            ws.bins[ws.tileStart[t] + pos] = f;
-        }
+    // as in the count: one atomic per distinct tile of the warp per round,
+    // the group's slots handed out by rank
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int rounds = __reduce_max_sync(act, nt);
+    for (int r = 0; r < rounds; ++r) {
+        const long long key = r < nt ? (long long)bc * T + (ty0 + r / w) * dims.tilesX + tx0 + r % w : -1ll;
+        const unsigned peers = __match_any_sync(act, key);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        int slot = 0;
+        if (key >= 0 && rank == 0) slot = atomicAdd(&ws.tileCursor[key], __popc(peers));
+        slot = __shfl_sync(act, slot, __ffs(peers) - 1) + rank;
+        if (key >= 0) ws.bins[ws.tileStart[key] + slot] = f;
+    }
 }
 
 // ---------------------------------------------------------------------------- single-call kernels
