@@ -204,6 +204,16 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     const float lo = zr1 ? __uint_as_float(~zr0) : kInf, hi = zr1 ? __uint_as_float(zr1) : 0.0f;
     const float scale = hi > lo ? (float)kBuckets / (hi - lo) : 0.0f;
     for (int k = tid; k <= kBuckets; k += kTilePix) sHist[k] = 0;
+    // the view's camera and SH coefficients, read by every pixel of the
+    // resolve and shading: staged once per tile
+    __shared__ Camera sCam;
+    __shared__ float sSH[27];
+    {
+        constexpr int kCamWords = (int)(sizeof(Camera) / sizeof(float));
+        if (tid < kCamWords) reinterpret_cast<float *>(&sCam)[tid] = reinterpret_cast<const float *>(ws.cams + bc)[tid];
+        else if (tid < kCamWords + 27) sSH[tid - kCamWords] = io.sh[(size_t)bc * 27 + (tid - kCamWords)];
+    }
+    if (nAll == 0) __syncthreads();  // (otherwise the first chunk's barriers order these stores)
     for (int c0 = 0; c0 < nAll; c0 += kChunk) {
         // Each thread builds one entry of the chunk and keeps it in registers
         // until its place in the front-to-back order is known: a counting
@@ -342,7 +352,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     if (u >= dims.W || v >= dims.H) return;
 
     // resolve: the reference's exact test on the candidates
-    const Camera &cam = ws.cams[bc];
+    const Camera &cam = sCam;
     ExactCtx x;
     x.geo = ws.geo + (size_t)b * F;
     x.vface = VF;
@@ -450,7 +460,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         const float k = phong_factor(ndl), s = phong_specular(ndl);
         col = make_float3(col.x * k + s, col.y * k + s, col.z * k + s);
     } else if (shaded) {
-        const float *sh = io.sh + (size_t)bc * 27;
+        const float *sh = sSH;
         float basis[9];
         sh_basis(n, basis);
         float l0 = 0.0f, l1 = 0.0f, l2 = 0.0f;
