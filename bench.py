@@ -545,7 +545,9 @@ def _fit_summary(ev, batch):
             "median_steps_to_goal": float(np.median([s for s in steps if s is not None])) if any(ok) else None,
             "median_gpu_ms_to_goal_per_fit": float(np.median(solved)) if solved else None,
             "mean_gpu_ms_to_solution_per_fit": float(np.mean([m if m is not None else per_fit_total for m in ms])),
-            "final_rmse_median": float(np.median(ev["final_rmse"])), "total_gpu_ms": ev["total_gpu_ms"]}
+            "final_rmse_median": float(np.median(ev["final_rmse"])), "total_gpu_ms": ev["total_gpu_ms"],
+            # the whole run's GPU time per fit that reaches the goal: what one solved fit costs
+            "gpu_ms_per_fit_reaching_goal": ev["total_gpu_ms"] / sum(ok) if any(ok) else None}
 
 
 def run_fit_bench(args):
@@ -592,6 +594,9 @@ def run_fit_bench(args):
                     value=ls["mean_gpu_ms_to_solution_per_fit"], config=cfg, learned=ls, plain=ps,
                     speedup_vs_plain=ps["mean_gpu_ms_to_solution_per_fit"] / ls["mean_gpu_ms_to_solution_per_fit"],
                     speedup_to_plain_final_rmse=float(t_p.mean() / t_l.mean()),
+                    speedup_per_fit_reaching_goal=(ps["gpu_ms_per_fit_reaching_goal"] / ls["gpu_ms_per_fit_reaching_goal"]
+                                                   if ps["gpu_ms_per_fit_reaching_goal"] and
+                                                   ls["gpu_ms_per_fit_reaching_goal"] else None),
                     training={"steps": steps, "seconds": secs, "loss": losses, "tc_error": tc.tc_error()})
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -143,9 +143,11 @@ class Trainer:
 def evaluate(fitter: fitting.Fitter, net: ProposalNet | None, seeds, steps=200, goal=0.01, fallback_step=20,
              fallback_rmse=0.05, batch=50):
     """Fits the targets of `seeds` (held-out parameter draws) from the
-    proposal (with the plain fit as fallback) or, with net=None, from the
-    mean.  Returns per-seed steps and GPU ms to RMSE <= goal (None if never),
-    the final RMSE, and the total GPU ms (all batches)."""
+    proposal (with the plain fit as fallback; refinement step sizes
+    Fitter.LR) or, with net=None, from the mean (step sizes
+    Fitter.LR_FROM_MEAN, which suit a far start).  Returns per-seed steps and
+    GPU ms to RMSE <= goal (None if never), the final RMSE, and the total GPU
+    ms (all batches)."""
     view_fitter = fitting.Fitter(fitter.model, num_views=4, size=VIEW) if net is not None else None
     steps_to, ms_to, final, curves, step_ms = [], [], [], [], []
     total_ms = 0.0
@@ -157,7 +159,7 @@ def evaluate(fitter: fitting.Fitter, net: ProposalNet | None, seeds, steps=200, 
             target = fitter.render(p)
         mean = fitting.mean_params(len(chunk))
         if net is None:
-            res = fitter.fit(target, mean, steps=steps, goal=goal)
+            res = fitter.fit(target, mean, steps=steps, goal=goal, lr=fitting.Fitter.LR_FROM_MEAN)
             extra_ms = 0.0
         else:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

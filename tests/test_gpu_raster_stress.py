@@ -80,3 +80,31 @@ def test_coplanar_duplicates_and_shared_edges():
     gpu = run_gpu(s)
     check_batch(s, gpu)
     assert np.all(gpu["face"][gpu["face"] >= 0] < F0)
+
+
+def test_long_slivers_across_warp_blocks():
+    """Long thin triangles at random angles: their boxes meet many 8x4 warp
+    blocks that the triangles themselves miss (the walk's ballot drops those
+    by a corner test), over a sphere that fills the frame behind them."""
+    rng = np.random.default_rng(11)
+    back = scenes.scene(720, 2, 96, 96, "vertexColor", "shaded", seed=11)
+    n = 300
+    c = rng.normal(0, 500, (n, 3))
+    d = rng.normal(0, 1, (n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    w = rng.normal(0, 1, (n, 3))
+    w -= (w * d).sum(1, keepdims=True) * d
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    width = rng.uniform(0.5, 8.0, (n, 1))
+    sl = np.stack([c - 700 * d, c + 700 * d, c + width * w], 1).reshape(-1, 3)
+    N0, F0 = back["num_vertices"], back["faces"].shape[0]
+    s = back
+    s["faces"] = np.concatenate([back["faces"], np.arange(3 * n, dtype=np.int32).reshape(-1, 3) + N0]).astype(np.int32)
+    s["uvs"] = np.concatenate([back["uvs"], rng.uniform(0, 1, (n, 6))]).astype(np.float32)
+    s["vertex_pos"] = np.concatenate([back["vertex_pos"], sl[None].astype(np.float32)], axis=1)
+    s["vertex_color"] = np.concatenate([back["vertex_color"], rng.uniform(0, 1, (1, 3 * n, 3)).astype(np.float32)],
+                                       axis=1)
+    s["num_vertices"] = s["vertex_pos"].shape[1]
+    gpu = run_gpu(s)
+    check_batch(s, gpu)
+    assert (gpu["face"] >= F0).any()   # some sliver is visible
