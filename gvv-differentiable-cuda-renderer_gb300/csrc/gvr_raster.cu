@@ -31,7 +31,7 @@ namespace {
 
 constexpr int kChunk = kTilePix;  // face entries staged per pass: one per thread
 constexpr int kBuckets = 256;     // depth buckets of the front-to-back order
-constexpr int kMaxCand = 4;       // candidates a pixel keeps in registers
+constexpr int kMaxCand = 7;       // candidates a pixel keeps in registers
 
 // Face entry with its skip-test constants and its box clipped to the tile
 // (80 bytes).  Fields are grouped in 16-byte rows in the order the walk
@@ -189,6 +189,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     // meshes at low resolution put thousands of faces in a tile); zup and
     // the candidates carry over from chunk to chunk.
     float zup = kInf;
+    int nLast = 0;  // kept entries of the last chunk (all of them when nAll <= kChunk)
     int nCand = 0;
     bool spill = false;
     int cf[kMaxCand];
@@ -234,6 +235,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
         __syncthreads();  // every warp is done walking the previous chunk; the histogram is clear
         if (keep) atomicAdd(&sHist[q], 1);
         const int nE = __syncthreads_count(keep);
+        nLast = nE;
         if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: kPer per lane, one warp scan
             constexpr int kPer = (kBuckets + 1 + 31) / 32;
             int h[kPer];
@@ -369,6 +371,22 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             if (j >= nCand || cz[j] > zup) continue;
             V3 t;
             const unsigned long long k = exact_key(x, cf[j], t, nLive > 1);
+            if (k < best) {
+                best = k;
+                abc = t;
+            }
+        }
+    } else if (nAll <= kChunk) {
+        // more candidates than registers, the tile's entries all still staged
+        // in front-to-back order: test those that may win against the final
+        // bound, up to the first whose bucket lies behind it
+        for (int e = 0; e < nLast; ++e) {
+            if (sBucketLo[e] > zup) break;
+            const Entry E = sE[e];
+            if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
+            if (!may_win(E, px, py, zup)) continue;
+            V3 t;
+            const unsigned long long k = exact_key(x, E.f, t, true);
             if (k < best) {
                 best = k;
                 abc = t;
