@@ -589,7 +589,7 @@ def run_fit_bench(args):
         ls["mean_gpu_ms_to_plain_final_rmse_per_fit"] = float(t_l.mean())
         ps["mean_gpu_ms_full_fit_per_fit"] = float(t_p.mean())
         cfg.update(train_renders=steps * batch, train_batch=batch,
-                   network="5 conv 3x3/2 (3-32-64-128-256-256) + MLP 16384-512-193, BF16 tcgen05 GEMMs, FP32 accum")
+                   network="5 conv 3x3/2 (3-32-64-128-256-256) + MLP 16384-1024-193, BF16 tcgen05 GEMMs, FP32 accum")
         line.update(metric="fit GPU ms to RMSE<=0.01 (learned proposal, per fit)",
                     value=ls["mean_gpu_ms_to_solution_per_fit"], config=cfg, learned=ls, plain=ps,
                     speedup_vs_plain=ps["mean_gpu_ms_to_solution_per_fit"] / ls["mean_gpu_ms_to_solution_per_fit"],

@@ -1,7 +1,7 @@
 """Learned proposal for analysis-by-synthesis fitting.
 
 A small CNN -- five 3x3 stride-2 convolutions (3 -> 32 -> 64 -> 128 -> 256
--> 256 channels) and a two-layer MLP (16384 -> 512 -> 193) -- regresses the
+-> 256 channels) and a two-layer MLP (16384 -> 1024 -> 193) -- regresses the
 morphable-model, pose and SH parameters of gvr.fitting from a 256 x 256
 render: the fitting views rendered at 128 x 128 and tiled 2 x 2.  Every
 matrix product of its forward and backward runs on the tcgen05 tensor-core
@@ -23,7 +23,7 @@ from . import fitting, tc
 from .fitting import N_PARAMS, PARAM_SLICES
 
 CHANNELS = (3, 32, 64, 128, 256, 256)
-HIDDEN = 512
+HIDDEN = 1024        # MLP width; held-out shape / albedo error after 800 steps 0.73 / 0.74 (512: 0.77 / 0.80)
 INPUT = 256          # network input edge (2 x 2 views of VIEW pixels)
 VIEW = 128
 
