@@ -224,7 +224,7 @@ def run_reference(args):
     value = P1 / (ms / 1e3) / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": min(args.warmup, 2), "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "batch": 1, "views": 8, "resolution": 1024, "faces": 70000,
                        "vertices": 35002, "texture": 1024, "parallelism": "replicas"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
