@@ -105,6 +105,8 @@ class Trainer:
         self.view_fitter = fitting.Fitter(model, num_views=4, size=VIEW)
         self.rng = np.random.default_rng(seed)
         self.opt = torch.optim.Adam(net.parameters(), lr=lr)
+        self.base_lr = [g["lr"] for g in self.opt.param_groups]
+        self.steps_done = 0
         self.active = (net.sd > 0).float()
 
     def sample(self, B):
@@ -124,20 +126,38 @@ class Trainer:
         self.opt.step()
         return loss
 
-    def train(self, steps, log_every=0, lr_final=0.05):
+    def train(self, steps, log_every=0, lr_final=0.05, start=0):
         """Adam with the step size decaying geometrically to lr_final times
-        its start; returns (losses, seconds)."""
-        base = [g["lr"] for g in self.opt.param_groups]
+        its start over `steps`, running steps start..steps-1 (start > 0
+        continues a run restored by resume()); returns (losses, seconds)."""
+        base = self.base_lr
         losses = []
         t0 = time.perf_counter()
-        for k in range(steps):
+        for k in range(start, steps):
             for g, b in zip(self.opt.param_groups, base):
                 g["lr"] = b * lr_final ** (k / max(steps, 1))
             loss = self.step()
+            self.steps_done = k + 1
             if log_every and (k % log_every == 0 or k == steps - 1):
-                losses.append((k, float(loss)))
+                losses.append((k, float(loss.detach())))
         torch.cuda.synchronize()
         return losses, time.perf_counter() - t0
+
+    def checkpoint(self, path):
+        """Weights, Adam state, the parameter sampler's RNG state and the
+        steps done, to `path` (torch.save)."""
+        torch.save({"weights": self.net.state(), "opt": self.opt.state_dict(), "base_lr": self.base_lr,
+                    "rng": self.rng.bit_generator.state, "steps_done": self.steps_done}, path)
+
+    def resume(self, path):
+        """Restores a checkpoint(); train(steps, start=self.steps_done) then
+        continues the run where it stopped."""
+        ck = torch.load(path, map_location="cpu", weights_only=False)
+        self.net.load(ck["weights"])
+        self.opt.load_state_dict(ck["opt"])
+        self.base_lr = list(ck["base_lr"])
+        self.rng.bit_generator.state = ck["rng"]
+        self.steps_done = int(ck["steps_done"])
 
 
 def evaluate(fitter: fitting.Fitter, net: ProposalNet | None, seeds, steps=200, goal=0.01, fallback_step=20,

@@ -38,3 +38,32 @@ def test_proposal_trains_and_beats_the_mean_start():
     err_mean = (((mean - p) / sd)[:, active] ** 2).mean()
     assert float(err_pred) < float(err_mean)
     assert float(rm_pred.mean()) < float(rm_mean.mean())
+
+
+def test_trainer_checkpoint_resume(tmp_path):
+    """A checkpoint restores the weights, the Adam state, the sampler's RNG
+    and the step count: the resumed trainer draws the same next batch and
+    holds the same optimiser state as the one that wrote it."""
+    import torch
+    from gvr import fitting, proposal
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    model = fitting.MorphableModel(num_vertices=2562, seed=0, device=dev)
+    a = proposal.Trainer(model, proposal.ProposalNet(dev, seed=0), batch=16, lr=1e-3, seed=3)
+    a.train(40)
+    path = tmp_path / "proposal.pt"
+    a.checkpoint(path)
+    b = proposal.Trainer(model, proposal.ProposalNet(dev, seed=5), batch=16, lr=2e-3, seed=9)
+    b.resume(path)
+    assert b.steps_done == a.steps_done == 40
+    for x, y in zip(a.net.parameters(), b.net.parameters()):
+        assert torch.equal(x.detach(), y.detach())
+    sa, sb = a.opt.state_dict(), b.opt.state_dict()
+    for k in sa["state"]:
+        for name in ("exp_avg", "exp_avg_sq"):
+            assert torch.equal(sa["state"][k][name].cpu(), sb["state"][k][name].cpu())
+    pa, _ = a.sample(4)
+    pb, _ = b.sample(4)
+    assert torch.equal(pa, pb)
+    losses, _ = b.train(50, start=b.steps_done)
+    assert b.steps_done == 50
