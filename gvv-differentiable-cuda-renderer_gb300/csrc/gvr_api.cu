@@ -135,6 +135,7 @@ BwdLayout bwd_layout(const GvrHandle *h, int B, void *base) {
     BwdLayout L{};
     L.s.cams = c.take<gvr::Camera>(BC);
     L.s.geo = c.take<gvr::FaceGeo>((size_t)B * h->F);
+    L.s.faceRec = c.take<float4>((size_t)B * h->F * gvr::kBwdFaceRows);
     L.s.faceAcc = c.take<float4>((size_t)B * h->F * (gvr::kFaceAccFloats / 4));
     L.s.gN = c.take<float4>((size_t)B * h->N);
     L.s.shPartial = c.take<float>(BC * T * 27);

@@ -162,7 +162,9 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
             }
         }
         if (f >= 0) {
-            const int i0 = topo.faces[3 * f], i1 = topo.faces[3 * f + 1], i2 = topo.faces[3 * f + 2];
+            const float4 *FR = ws.faceRec + ((size_t)b * F + f) * kBwdFaceRows;  // the face's record
+            const float4 fr0 = FR[0];
+            const int i0 = __float_as_int(fr0.x), i1 = __float_as_int(fr0.y), i2 = __float_as_int(fr0.z);
             const float *VN = io.vnormal + (size_t)bc * N * 3;
             const V3 N0 = ld3(VN + 3 * i0), N1 = ld3(VN + 3 * i1), N2 = ld3(VN + 3 * i2);
             const V3 un = pixel_normal_un(N0, N1, N2, abc);
@@ -198,7 +200,8 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
                     alb[ch] = abc.x * Cb[3 * i0 + ch] + abc.y * Cb[3 * i1 + ch] + abc.z * Cb[3 * i2 + ch];
             }
             if (MODE == GVR_ALBEDO_TEXTURED) {
-                const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+                const float4 fr1 = FR[1];
+                const float2 tc = texel_coord6(fr0.w, fr1.x, fr1.y, fr1.z, fr1.w, FR[2].x, abc, dims.Wt, dims.Ht);
                 const int iu = __float2int_rz(xs(tc.x, 0.5f)), iv = __float2int_rz(xs(tc.y, 0.5f));
                 const int hu = min(iu + 1, dims.Wt - 1), hv = min(iv + 1, dims.Ht - 1);
                 const float LU = iu + 0.5f, HU = iu + 1.5f, LV = iv + 0.5f, HV = iv + 1.5f;
@@ -215,7 +218,8 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
                               G[1] * JCoAl[1], G[2] * JCoAl[2]);
             }
             if (MODE == GVR_ALBEDO_TEXTURED_BILINEAR) {  // the lookup and its derivative: four texels
-                const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+                const float4 fr1 = FR[1];
+                const float2 tc = texel_coord6(fr0.w, fr1.x, fr1.y, fr1.z, fr1.w, FR[2].x, abc, dims.Wt, dims.Ht);
                 int idx[4];
                 float w[4];
                 bilinear_taps(tc.x, tc.y, dims.Wt, dims.Ht, idx, w);
@@ -270,10 +274,10 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
                 }
             }
             if (SHADED || ALBPOS) {
-                const float *Vb = io.verts + (size_t)b * N * 3;
-                const float3 V0 = make_float3(Vb[3 * i0], Vb[3 * i0 + 1], Vb[3 * i0 + 2]);
-                const float3 e1 = make_float3(Vb[3 * i1] - V0.x, Vb[3 * i1 + 1] - V0.y, Vb[3 * i1 + 2] - V0.z);
-                const float3 e2 = make_float3(Vb[3 * i2] - V0.x, Vb[3 * i2 + 1] - V0.y, Vb[3 * i2 + 2] - V0.z);
+                const float4 fr2 = FR[2], fr3 = FR[3], fr4 = FR[4];  // vertex positions
+                const float3 V0 = make_float3(fr2.y, fr2.z, fr2.w);
+                const float3 e1 = make_float3(fr3.x - V0.x, fr3.y - V0.y, fr3.z - V0.z);
+                const float3 e2 = make_float3(fr3.w - V0.x, fr4.x - V0.y, fr4.y - V0.z);
                 const float Nf[3] = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
                 // N.d and the hit point in compensated arithmetic: near grazing
                 // incidence both cancel badly in plain FP32 (error ~ eps/cos) and
@@ -336,10 +340,11 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
                         }
                     gu /= norm;
                     gv /= norm;
-                    const float *Vb = io.verts + (size_t)b * N * 3;
+                    const float4 fr2 = FR[2], fr3 = FR[3], fr4 = FR[4];  // vertex positions
+                    const float P0[3] = {fr2.y, fr2.z, fr2.w}, P1[3] = {fr3.x, fr3.y, fr3.z}, P2[3] = {fr3.w, fr4.x, fr4.y};
                     float X[3];
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) X[a] = abc.x * Vb[3 * i0 + a] + abc.y * Vb[3 * i1 + a] + abc.z * Vb[3 * i2 + a];
+                    for (int a = 0; a < 3; ++a) X[a] = abc.x * P0[a] + abc.y * P1[a] + abc.z * P2[a];
                     const float *KE = cam.KE;
                     const float Px = KE[0] * X[0] + KE[1] * X[1] + KE[2] * X[2] + KE[3];
                     const float Py = KE[4] * X[0] + KE[5] * X[1] + KE[6] * X[2] + KE[7];
@@ -552,7 +557,7 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     if ((err = cudaMemsetAsync(ws.faceAcc, 0, (size_t)B * F * kFaceAccFloats * sizeof(float), st))) return err;
     if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
     if ((err = launch_cameras(a.extrinsics, a.intrinsics, ws.cams, B * C, st))) return err;
-    if ((err = launch_face_geo(a.vertex_pos, topo, ws.geo, nullptr, B, st))) return err;
+    if ((err = launch_face_geo(a.vertex_pos, topo, ws.geo, nullptr, B, st, ws.faceRec))) return err;
     const int phong = dims.shading == GVR_SHADING_PHONG && dims.albedo != GVR_ALBEDO_FOREGROUND_MASK;
     BwdIO io{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image, a.vertex_normal,
              a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter, phong};

@@ -117,13 +117,27 @@ __device__ __forceinline__ void camera_item(const float *__restrict__ extr, cons
 
 // ---------------------------------------------------------------------------- face setup
 
+// rec (backward only, else null): the face's BwdScratch::faceRec record;
+// uvs may be null (no texture coordinates: zeros).
 __device__ __forceinline__ void face_geo_item(const float *__restrict__ verts, const int32_t *__restrict__ faces,
                                               FaceGeo *__restrict__ geo, float4 *__restrict__ fnormal, int N, int F,
-                                              int i) {
+                                              int i, float4 *__restrict__ rec = nullptr,
+                                              const float *__restrict__ uvs = nullptr) {
     int b = i / F, f = i - b * F;
     const float *V = verts + (size_t)b * N * 3;
     int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
     V3 p0 = ld3(V + 3 * i0), p1 = ld3(V + 3 * i1), p2 = ld3(V + 3 * i2);
+    if (rec) {
+        float t[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (uvs)
+            for (int k = 0; k < 6; ++k) t[k] = uvs[6 * (size_t)f + k];
+        float4 *R = rec + (size_t)i * kBwdFaceRows;
+        R[0] = make_float4(__int_as_float(i0), __int_as_float(i1), __int_as_float(i2), t[0]);
+        R[1] = make_float4(t[1], t[2], t[3], t[4]);
+        R[2] = make_float4(t[5], p0.x, p0.y, p0.z);
+        R[3] = make_float4(p1.x, p1.y, p1.z, p2.x);
+        R[4] = make_float4(p2.y, p2.z, 0.0f, 0.0f);
+    }
     V3 fn = xcross(xsub(p1, p0), xsub(p2, p0));
     if (fnormal) fnormal[i] = make_float4(fn.x, fn.y, fn.z, 0.0f);
     // rayTriangleIntersect scales vertices by 1/1000 (RendererUtil.h:29-32)
@@ -399,9 +413,10 @@ __global__ void k_cameras(const float *__restrict__ extr, const float *__restric
 }
 
 __global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__restrict__ faces, FaceGeo *__restrict__ geo,
-                           float4 *__restrict__ fnormal, int N, int F, int B) {
+                           float4 *__restrict__ fnormal, int N, int F, int B, float4 *__restrict__ rec,
+                           const float *__restrict__ uvs) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < B * F) face_geo_item(verts, faces, geo, fnormal, N, F, i);
+    if (i < B * F) face_geo_item(verts, faces, geo, fnormal, N, F, i, rec, uvs);
 }
 
 __global__ void k_vertices(const FwdJob J) {
@@ -475,10 +490,10 @@ cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, i
 }
 
 cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *geo, float4 *fnormal, int B,
-                            cudaStream_t st) {
+                            cudaStream_t st, float4 *bwdRec) {
     GVR_LAUNCH(st, "k_face_geo",
                k_face_geo<<<blocks((size_t)B * topo.F, 256), 256, 0, st>>>(verts, topo.faces, geo, fnormal, topo.N,
-                                                                            topo.F, B));
+                                                                            topo.F, B, bwdRec, topo.uvs));
     return cudaGetLastError();
 }
 

@@ -193,10 +193,11 @@ __device__ __forceinline__ V3 pixel_normal_un(V3 n0, V3 n1, V3 n2, V3 abc) {
 
 // Nearest-texel texture coordinate (CUDABasedRasterization.cu:326-345):
 // returns the clamped (U0, V0) in texels.
-__device__ __forceinline__ float2 texel_coord(const float *uv6, V3 abc, int Wt, int Ht) {
-    float t0x = uv6[0], t0y = xs(1.0f, uv6[1]);
-    float t1x = uv6[2], t1y = xs(1.0f, uv6[3]);
-    float t2x = uv6[4], t2y = xs(1.0f, uv6[5]);
+__device__ __forceinline__ float2 texel_coord6(float u0, float v0, float u1, float v1, float u2, float v2, V3 abc,
+                                              int Wt, int Ht) {
+    float t0x = u0, t0y = xs(1.0f, v0);
+    float t1x = u1, t1y = xs(1.0f, v1);
+    float t2x = u2, t2y = xs(1.0f, v2);
     float fx = xa(xa(xm(t0x, abc.x), xm(t1x, abc.y)), xm(t2x, abc.z));
     float fy = xa(xa(xm(t0y, abc.x), xm(t1y, abc.y)), xm(t2y, abc.z));
     fx = xm(fx, (float)Wt);
@@ -204,6 +205,10 @@ __device__ __forceinline__ float2 texel_coord(const float *uv6, V3 abc, int Wt, 
     fx = fminf(fmaxf(fx, 0.0f), (float)(Wt - 1));
     fy = fminf(fmaxf(fy, 0.0f), (float)(Ht - 1));
     return make_float2(fx, fy);
+}
+
+__device__ __forceinline__ float2 texel_coord(const float *uv6, V3 abc, int Wt, int Ht) {
+    return texel_coord6(uv6[0], uv6[1], uv6[2], uv6[3], uv6[4], uv6[5], abc, Wt, Ht);
 }
 
 // SH irradiance per channel (getIllum, cpp/src/Utils/RendererUtil.h:179-214).
@@ -345,9 +350,17 @@ struct FwdJob {
     float *vnormal_out;  // [B,C,N,3] (the buffer io.vnormal reads)
 };
 
+// Per (batch, face) record of what the backward's pixels read about their
+// face, five 16-byte rows instead of 18 scalar gathers:
+//   r0 = i0, i1, i2 (int bits), u0;  r1 = v0, u1, v1, u2;  r2 = v2, V0.xyz;
+//   r3 = V1.xyz, V2.x;  r4 = V2.yz, 0, 0   (u, v: texture coordinates as
+// stored; V: vertex positions, mm).
+constexpr int kBwdFaceRows = 5;
+
 struct BwdScratch {
     Camera *cams;        // [B*C]
     FaceGeo *geo;        // [B*F]
+    float4 *faceRec;     // [B*F*kBwdFaceRows]
     float4 *faceAcc;     // [B*F*kFaceAccFloats/4]
     float4 *gN;          // [B*N] normal-gradient accumulator per vertex
     float *shPartial;    // [B*C*T*27]

@@ -24,7 +24,7 @@ struct BatchLaunch {
 
 cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, int count, cudaStream_t st);
 cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *geo, float4 *fnormal, int B,
-                            cudaStream_t st);
+                            cudaStream_t st, float4 *bwdRec = nullptr);
 cudaError_t launch_forward(const FwdJob &J, cudaStream_t st);
 cudaError_t launch_forward_normal_map(const FwdJob &J, int *uvOwner, float *normal_map, cudaStream_t st);
 cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st);

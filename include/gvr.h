@@ -192,7 +192,7 @@ int gvr_debug_rays(GvrHandle *handle, int32_t batch, const float *extrinsics, co
  * backward needs (per-face gradient accumulators, SH partial sums, camera and
  * face records) lives in one device array of GVR_NOALLOC_SCRATCH_BYTES that
  * the library reserves on each GPU it is loaded on, for the life of the
- * process.  Calls needing more scratch than that (about 17 MiB for one batch
+ * process.  Calls needing more scratch than that (about 22 MiB for one batch
  * element of 8 views at 1024x1024 and 70,000 faces) return
  * GVR_ERR_WORKSPACE.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress), so make that first call before any stream
