@@ -5,9 +5,12 @@
 //
 // The reference tests every pixel of every face's box with its FP32
 // world-space ray/triangle test and keeps the smallest quantised depth.
-// Here each thread owns one pixel; the tile's face entries are staged in
-// shared memory, sorted front to back by a lower bound of their depth, and
-// each warp walks them once with cheap screen-space bounds:
+// Here each thread owns one pixel and each warp an 8x4 block of the tile;
+// the tile's face entries are staged in shared memory, counting-sorted front
+// to back into depth buckets spanning the view's range of depth lower bounds,
+// and each warp walks them once -- 32 at a time, a ballot keeping only the
+// entries whose triangle may cover a pixel centre of its block -- with cheap
+// screen-space bounds:
 //
 //   - a face that certainly covers the pixel lowers the pixel's depth bound
 //     zup (the face's exact quantised depth is <= zup);
