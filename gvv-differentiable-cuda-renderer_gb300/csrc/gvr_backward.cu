@@ -13,8 +13,12 @@
 //                  col_j = b_j * c         vertex colour
 //                The warp pre-reduces them per face id (__match_any_sync +
 //                a shuffle tree) and one lane per face adds them to a per-face
-//                accumulator with 16-byte vector atomics.  SH gradients are
-//                block-reduced into per-tile partials; texels get atomics.
+//                accumulator with 16-byte vector atomics.  SH gradients go
+//                through a warp reduce-scatter into per-tile partials;
+//                texels get atomics.  What a pixel reads about its face
+//                (vertex indices, texture coordinates, vertex positions)
+//                comes from one 80-byte record per face that the face pass
+//                (k_face_geo) writes.
 //  k_gather_a    per vertex, over its CSR faces: colour grad, position grad
 //                (direct terms) and the vertex-normal gradient gN[v].
 //  k_gather_b    per vertex: the normal-adjacency term of :559-615.  The
