@@ -108,3 +108,31 @@ def test_long_slivers_across_warp_blocks():
     gpu = run_gpu(s)
     check_batch(s, gpu)
     assert (gpu["face"] >= F0).any()   # some sliver is visible
+
+
+def test_stacked_coplanar_layers_overflow_the_register_candidates():
+    """Ten copies of every face: each covered pixel has ten candidates of
+    equal depth, more than a pixel keeps in registers, so the resolve takes
+    the slow path over the tile's staged entries; ties go to the smallest
+    face id."""
+    s = scenes.scene(720, 2, 64, 64, "vertexColor", "shaded", seed=12)
+    F0 = s["faces"].shape[0]
+    s["faces"] = np.concatenate([s["faces"]] * 10).astype(np.int32)
+    s["uvs"] = np.concatenate([s["uvs"]] * 10).astype(np.float32)
+    gpu = run_gpu(s)
+    check_batch(s, gpu)
+    assert np.all(gpu["face"][gpu["face"] >= 0] < F0)
+
+
+def test_dense_tiles_go_through_shared_memory_in_chunks():
+    """A 40,000-face sphere at 48x48: a 16x16 tile holds thousands of face
+    entries, staged and walked 256 at a time (and, with three stacked
+    copies, resolved by the slow path over the bins)."""
+    s = scenes.scene(40000, 1, 48, 48, "vertexColor", "shaded", seed=13)
+    check_batch(s, run_gpu(s), grads=False)
+    F0 = s["faces"].shape[0]
+    s["faces"] = np.concatenate([s["faces"]] * 3).astype(np.int32)
+    s["uvs"] = np.concatenate([s["uvs"]] * 3).astype(np.float32)
+    gpu = run_gpu(s)
+    check_batch(s, gpu, grads=False)
+    assert np.all(gpu["face"][gpu["face"] >= 0] < F0)
