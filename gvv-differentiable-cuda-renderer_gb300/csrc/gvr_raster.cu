@@ -33,7 +33,7 @@ namespace gvr {
 namespace {
 
 constexpr int kChunk = kTilePix;  // face entries staged per pass: one per thread
-constexpr int kBuckets = 256;     // depth buckets of the front-to-back order
+constexpr int kBuckets = 128;     // depth buckets of the front-to-back order
 constexpr int kMaxCand = 7;       // candidates a pixel keeps in registers
 
 // Face entry with its skip-test constants and its box clipped to the tile
