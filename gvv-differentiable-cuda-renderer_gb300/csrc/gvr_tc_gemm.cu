@@ -60,12 +60,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Waits for the phase with `parity` to complete, at most ~1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Waits for the phase with `parity` to complete, at most limit_ns (~1 s).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = 1000000000ull) {
     const uint64_t t0 = global_ns();
     while (!mbar_try_wait(bar, parity))
-        if (global_ns() - t0 > 1000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     return true;
+}
+
+// Test hook of the bounded waits: one warp waits on an mbarrier that nothing
+// arrives on, gives up after limit_ns, records error code 2 and returns (no
+// tensor memory or MMA involved, so nothing is left in flight).
+__global__ void k_tc_wait_probe(unsigned long long limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const bool done = mbar_wait(&bar, 0, limit_ns);
+    if (!done && threadIdx.x == 0) atomicExch(&g_tc_error, 2);
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -320,6 +331,15 @@ int gvr_tc_error(int clear) {
         cudaMemcpyToSymbol(gvr::g_tc_error, &z, sizeof(int));
     }
     return v;
+}
+
+int gvr_tc_wait_probe(unsigned long long limit_ns, void *stream) {
+    if (limit_ns == 0 || limit_ns > 2000000000ull)
+        return nn_fail(GVR_ERR_INVALID_ARGUMENT, "wait probe: limit must be in (0, 2 s]");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    gvr::k_tc_wait_probe<<<1, 32, 0, st>>>(limit_ns);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GVR_OK : nn_fail(GVR_ERR_CUDA, cudaGetErrorString(e));
 }
 
 int gvr_im2col_3x3s2(const void *x, void *col, int B, int H, int W, int Cin, int Kpad, void *stream) {

@@ -67,7 +67,7 @@ EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forw
            "gvr_plan_create", "gvr_plan_forward", "gvr_plan_forward_graph", "gvr_plan_tile_config",
            "gvr_plan_destroy", "gvr_image_gradient", "gvr_image_gaussian3x3",
            # include/gvr_nn.h
-           "gvr_gemm_bf16", "gvr_tc_error", "gvr_im2col_3x3s2", "gvr_col2im_3x3s2", "gvr_nn_last_error")
+           "gvr_gemm_bf16", "gvr_tc_error", "gvr_tc_wait_probe", "gvr_im2col_3x3s2", "gvr_col2im_3x3s2", "gvr_nn_last_error")
 
 NOALLOC_SCRATCH_BYTES = 32 << 20  # GVR_NOALLOC_SCRATCH_BYTES
 

@@ -47,6 +47,8 @@ def _lib_nn():
         L.gvr_gemm_bf16.restype = ctypes.c_int
         L.gvr_tc_error.argtypes = [ctypes.c_int]
         L.gvr_tc_error.restype = ctypes.c_int
+        L.gvr_tc_wait_probe.argtypes = [ctypes.c_ulonglong, ctypes.c_void_p]
+        L.gvr_tc_wait_probe.restype = ctypes.c_int
         L.gvr_im2col_3x3s2.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 5 + [ctypes.c_void_p]
         L.gvr_im2col_3x3s2.restype = ctypes.c_int
         L.gvr_col2im_3x3s2.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 5 + [ctypes.c_void_p]
@@ -106,6 +108,12 @@ def gemm(A, B, bias=None, relu=False, out_dtype=torch.float32):
 def tc_error(clear=True):
     """Nonzero if a GEMM timed out waiting for its tensor-core work."""
     return int(_lib_nn().gvr_tc_error(1 if clear else 0))
+
+
+def wait_probe(limit_ms, device):
+    """Runs the bounded-wait test hook (an mbarrier wait that nothing ends,
+    given up after `limit_ms`) on `device`'s current stream."""
+    _check(_lib_nn().gvr_tc_wait_probe(int(limit_ms * 1e6), _stream(torch.device(device))))
 
 
 def im2col(x, kpad):

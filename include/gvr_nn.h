@@ -50,6 +50,12 @@ int gvr_gemm_bf16(const GvrGemmArgs *args, void *stream);
  * its tile unwritten); `clear` resets the flag.  -1 if it cannot be read. */
 int gvr_tc_error(int clear);
 
+/* Test hook of the bounded waits that gvr_tc_error reports: one warp waits
+ * on an mbarrier that nothing arrives on, gives up after limit_ns
+ * (0 < limit_ns <= 2e9), sets the flag to 2 and returns; the context stays
+ * usable.  Asynchronous on `stream`. */
+int gvr_tc_wait_probe(unsigned long long limit_ns, void *stream);
+
 /* im2col of a 3x3, stride-2, padding-1 convolution: x NHWC BF16 [B,H,W,Cin]
  * -> col BF16 [B*Ho*Wo, Kpad] with Ho = ceil(H/2), Wo = ceil(W/2), column
  * (ky*3 + kx)*Cin + c, columns >= 9*Cin zero. */

@@ -123,3 +123,29 @@ def test_conv_and_linear_layers_match_fp32_reference():
     assert _rel(xl.grad, xq.grad) <= 1e-2
     assert _rel(wl.grad, wq.grad) <= 1e-2
     assert tc.tc_error() == 0
+
+
+def test_bounded_wait_times_out_and_leaves_the_context_usable():
+    """A kernel waiting on an mbarrier that nothing arrives on gives up after
+    its limit and reports it through gvr_tc_error; the GEMM still works and
+    the flag stays clear afterwards."""
+    import torch
+    from gvr import tc
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    tc.tc_error(clear=True)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    tc.wait_probe(5.0, dev)
+    t1.record()
+    t1.synchronize()
+    assert tc.tc_error(clear=True) == 2
+    assert t0.elapsed_time(t1) >= 4.0       # it did wait about its limit
+    A = torch.randn(128, 64, device=dev).to(torch.bfloat16)
+    B = torch.randn(64, 64, device=dev).to(torch.bfloat16)
+    C = tc.gemm(A, B)
+    torch.cuda.synchronize()
+    ref = A.float() @ B.float().t()
+    assert torch.allclose(C, ref, rtol=2e-3, atol=2e-3)
+    assert tc.tc_error(clear=False) == 0
