@@ -89,3 +89,32 @@ def test_error_status_raises(lib):
     with pytest.raises(_lib.GvrError) as ei:
         _lib.check(lib.gvr_forward(None, None, None))
     assert ei.value.status == -1
+
+
+def _header_constants():
+    """Enumerators and #defines of include/gvr.h as a name -> int map."""
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gvr.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for name, val in re.findall(r"\b(GVR_[A-Z0-9_]+)\s*=\s*(-?\d+)", src):
+        out[name] = int(val)
+    for m in re.finditer(r"#define\s+(GVR_[A-Z0-9_]+)\s+\(?(\d+)u?(?:\s*<<\s*(\d+))?\)?", src):
+        out[m.group(1)] = int(m.group(2)) << int(m.group(3) or 0)
+    return out
+
+
+def test_python_constants_match_the_header():
+    from gvr import _lib
+    h = _header_constants()
+    camel = {"VERTEX_COLOR": "vertexColor", "TEXTURED": "textured", "NORMAL": "normal", "LIGHTING": "lighting",
+             "FOREGROUND_MASK": "foregroundMask", "TEXTURED_BILINEAR": "texturedBilinear", "UV": "uv"}
+    for suffix, name in camel.items():
+        assert _lib.ALBEDO[name] == h["GVR_ALBEDO_" + suffix], name
+    for name in ("shaded", "shadeless", "phong"):
+        assert _lib.SHADING[name] == h["GVR_SHADING_" + name.upper()], name
+    for code, name in _lib.STATUS.items():
+        assert h[name] == code, name
+    assert _lib.BACKWARD_ALBEDO_POSITION == h["GVR_BACKWARD_ALBEDO_POSITION"]
+    assert _lib.PLAN_AUTOTUNE == h["GVR_PLAN_AUTOTUNE"]
+    assert _lib.NOALLOC_SCRATCH_BYTES == h["GVR_NOALLOC_SCRATCH_BYTES"]
