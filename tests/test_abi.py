@@ -93,8 +93,7 @@ def test_error_status_raises(lib):
 
 def _header_constants():
     """Enumerators and #defines of include/gvr.h as a name -> int map."""
-    import re
-    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gvr.h")).read()
+    src = open(os.path.join(REPO, "include", "gvr.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     out = {}
     for name, val in re.findall(r"\b(GVR_[A-Z0-9_]+)\s*=\s*(-?\d+)", src):
