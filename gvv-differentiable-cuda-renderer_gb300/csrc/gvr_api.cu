@@ -441,22 +441,32 @@ int gvr_debug_rays(GvrHandle *h, int32_t batch, const float *extr, const float *
 //
 // Scratch for gvr_backward_noalloc: a fixed device array that every GPU
 // loading this library holds until the process exits.  In host code the
-// symbol is only a stand-in, so its device address is looked up once per
-// device (with that device current) and cached.
+// symbol is only a stand-in, so its device address is looked up (with the
+// handle's device current) on every call: the lookup is a table read once
+// the module is loaded, and a device reset, after which the module is
+// loaded again and the array may move, cannot leave a stale address behind.
+// The first call on a device loads the module, so it should come before
+// any stream capture.
 
 namespace {
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[GVR_NOALLOC_SCRATCH_BYTES];
 
-std::mutex g_noalloc_mu;
-std::vector<void *> g_noalloc_addr;  // per device ordinal
-
 }  // namespace
 
 extern "C" int gvr_backward_noalloc(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
     if (!h || !a) return fail(GVR_ERR_INVALID_ARGUMENT, "handle/args is NULL");
+    if (!batch_fits(h, a->batch))
+        return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1 and the call within int32 index range");
+    const int mode = h->attrs.albedo_mode;
+    if (mode == GVR_ALBEDO_NORMAL || mode == GVR_ALBEDO_LIGHTING || mode == GVR_ALBEDO_UV) {
+        // zero-gradient modes only clear the outputs: no scratch at all
+        GvrBackwardArgs args = *a;
+        args.workspace = nullptr;
+        args.workspace_bytes = 0;
+        return gvr_backward(h, &args, stream);
+    }
     const size_t need = gvr_backward_workspace_size(h, a->batch, a->texture_height, a->texture_width);
-    if (need == 0) return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1");
     if (need > GVR_NOALLOC_SCRATCH_BYTES)
         return fail(GVR_ERR_WORKSPACE, "gvr_backward_noalloc: this call needs " + std::to_string(need) +
                                            " bytes of scratch but the library's fixed scratch array holds " +
@@ -466,16 +476,8 @@ extern "C" int gvr_backward_noalloc(GvrHandle *h, const GvrBackwardArgs *a, void
     {
         DeviceGuard g(h->device);
         if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (h->device < 0) return fail(GVR_ERR_INVALID_ARGUMENT, "bad device");
-        if ((size_t)h->device >= g_noalloc_addr.size()) g_noalloc_addr.resize(h->device + 1, nullptr);
-        if (!g_noalloc_addr[h->device]) {
-            void *p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
-            g_noalloc_addr[h->device] = p;
-        }
-        scratch = g_noalloc_addr[h->device];
+        const cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
     }
     GvrBackwardArgs args = *a;
     args.workspace = scratch;

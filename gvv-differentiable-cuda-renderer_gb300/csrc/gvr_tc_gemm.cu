@@ -19,9 +19,12 @@
 //   * the epilogue waits for the last commit, reads the accumulator with
 //     tcgen05.ld (warp w owns lanes 32w..32w+31 = rows), adds the bias,
 //     applies ReLU and stores.
-// Every mbarrier wait is bounded (about one second of %globaltimer): on
-// timeout the kernel records an error code in g_tc_error, waits once more
-// (bounded) for its MMAs, frees its tensor memory and returns.
+// Every mbarrier wait is bounded (about one second of %globaltimer) and is
+// done by thread 0 alone; the block then agrees on the outcome with
+// __syncthreads_and, so every thread leaves the K loop, skips the epilogue
+// and reaches the tensor-memory free together.  On timeout the kernel
+// records an error code in g_tc_error, waits once more (bounded) for its
+// MMAs, frees its tensor memory and returns.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -140,14 +143,19 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
     const int KTall = K / kBK, per = (KTall + gridDim.z - 1) / gridDim.z;
     const int ktBegin = blockIdx.z * per, ktEnd = min(KTall, ktBegin + per);
     const int KT = max(0, ktEnd - ktBegin);
-    uint32_t parity[kStages] = {0u, 0u};
+    // The commit of step j arrives on mbar[j % 2]; it completes that
+    // barrier's phase j / 2, so its wait parity is (j / 2) & 1.
     bool ok = true;
-    for (int kt = 0; kt < KT && ok; ++kt) {
+    int issued = 0;  // steps whose MMAs were committed
+    for (int kt = 0; kt < KT; ++kt) {
         const int s = kt & 1;
         if (kt >= kStages) {  // the MMAs of step kt - 2 read this stage
-            ok = mbar_wait(&mbar[s], parity[s]);
-            parity[s] ^= 1u;
-            if (!ok) break;
+            bool done = true;
+            if (tid == 0) done = mbar_wait(&mbar[s], ((kt - kStages) >> 1) & 1);
+            if (!__syncthreads_and(done)) {  // one decision for the whole block
+                ok = false;
+                break;
+            }
         }
         const int k0 = (ktBegin + kt) * kBK;
         load_tile(sA + s * kTileBytes, A, m0, M, k0, lda);
@@ -178,16 +186,20 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
                              smem_u32(&mbar[s]))
                          : "memory");
         }
+        issued = kt + 1;
     }
     // the last commit tracks every MMA issued before it
-    if (KT > 0) {
-        const int s = (KT - 1) & 1;
-        const bool done = mbar_wait(&mbar[s], parity[s]);
-        if (!done || !ok) {
-            if (lane == 0) atomicExch(&g_tc_error, 1);
-            mbar_wait(&mbar[s], parity[s]);
-            ok = false;
+    if (issued > 0) {
+        const int j = issued - 1;
+        bool done = true;
+        if (tid == 0) {
+            done = ok && mbar_wait(&mbar[j & 1], (j >> 1) & 1);
+            if (!done) {  // record, then give the MMAs in flight one more bounded wait before the free
+                atomicExch(&g_tc_error, 1);
+                mbar_wait(&mbar[j & 1], (j >> 1) & 1);
+            }
         }
+        ok = __syncthreads_and(done) != 0;
     }
     tc_fence_after();
 

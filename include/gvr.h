@@ -194,11 +194,15 @@ int gvr_debug_rays(GvrHandle *handle, int32_t batch, const float *extrinsics, co
  * the library reserves on each GPU it is loaded on, for the life of the
  * process.  Calls needing more scratch than that (about 22 MiB for one batch
  * element of 8 views at 1024x1024 and 70,000 faces) return
- * GVR_ERR_WORKSPACE.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  Every call on a device shares the one array: calls that overlap
- * on the GPU (other streams, other threads) race and corrupt each other's
- * results; everything that must start at zero is cleared inside each call. */
+ * GVR_ERR_WORKSPACE (the normal, lighting and UV modes need no scratch and
+ * take any size).  Each call looks up the array's device address
+ * (cudaGetSymbolAddress) with the handle's device current; the first call on
+ * a device also loads the library's device code there, so make that first
+ * call before any stream capture.  A device reset invalidates handles, not
+ * this lookup.  Every call on a device shares the one array: calls that
+ * overlap on the GPU (other streams, other threads) race and corrupt each
+ * other's results; everything that must start at zero is cleared inside
+ * each call. */
 #define GVR_NOALLOC_SCRATCH_BYTES (32u << 20)
 int gvr_backward_noalloc(GvrHandle *handle, const GvrBackwardArgs *args, void *stream);
 

@@ -23,9 +23,10 @@ import subprocess
 
 import numpy as np
 
+from .refsrc import reference_path
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(_HERE, "_ref")
-REFERENCE = "/root/reference"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FATBINS = {"fwd": "CUDABasedRasterization.cu", "bwd": "CUDABasedRasterizationGrad.cu"}
 
@@ -40,11 +41,11 @@ def _fatbin(kind, fmad):
 
 def build_fatbins():
     """Compile the reference kernels (needs the reference sources)."""
-    src = os.path.join(REFERENCE, "cpp", "src")
+    src = reference_path("cpp", "src")
     if not os.path.isdir(src):
         return False
     os.makedirs(REF_DIR, exist_ok=True)
-    inc = ["-I", os.path.join(REFERENCE, "cpp", "thirdParty", "Shared", "cutil", "inc"), "-I",
+    inc = ["-I", reference_path("cpp", "thirdParty", "Shared", "cutil", "inc"), "-I",
            os.path.join(src, "Utils"), "-I", os.path.join(src, "Renderer")]
     for kind, fname in FATBINS.items():
         for fmad in (True, False):
@@ -110,13 +111,13 @@ def build_uvmap_ref():
     cpp/src/Renderer/CUDABasedRasterization.cpp (unchanged, plus the same
     clockRate shim) and refcore/uvmap_ref.cpp.  Only where the reference
     sources are present; needs no GPU."""
-    src = os.path.join(REFERENCE, "cpp", "src")
+    src = reference_path("cpp", "src")
     if not os.path.isdir(src):
         return False
     os.makedirs(REF_DIR, exist_ok=True)
     cuda = os.path.dirname(os.path.dirname(_nvcc()))
     inc = ["-I", os.path.join(cuda, "include"), "-I",
-           os.path.join(REFERENCE, "cpp", "thirdParty", "Shared", "cutil", "inc"), "-I", os.path.join(src, "Utils"),
+           reference_path("cpp", "thirdParty", "Shared", "cutil", "inc"), "-I", os.path.join(src, "Utils"),
            "-I", os.path.join(src, "Renderer")]
     subprocess.run(["g++", "-O2", "-fPIC", "-fopenmp", "-w", "-shared", "-DclockRate=l2CacheSize", *inc, "-o",
                     UVMAP_LIB, os.path.join(src, "Renderer", "CUDABasedRasterization.cpp"),

@@ -13,7 +13,9 @@ import zlib
 import numpy as np
 import pytest
 
-REF_DATA = "/root/reference/python/data"
+from oracle.refsrc import reference_data
+
+REF_DATA = reference_data()
 
 
 def _write_png_filtered(path, img8, filters):

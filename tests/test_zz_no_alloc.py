@@ -20,12 +20,12 @@ pytestmark = pytest.mark.gpu
 GRAD_TOL = 1e-4
 
 
-def _setup(albedo, shading):
+def _setup(albedo, shading, batch=1):
     import torch
     from gvr import renderer
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    s = small_scene(num_faces=1280, views=2, size=64, albedo=albedo, shading=shading, tex=16, seed=41)
+    s = small_scene(num_faces=1280, views=2, size=64, albedo=albedo, shading=shading, tex=16, seed=41, batch=batch)
     rng = np.random.default_rng(41)
     s["target_image"] = rng.uniform(0, 1, s["target_image"].shape).astype(np.float32)
     s["grad_target"] = rng.normal(0, 1, s["grad_target"].shape).astype(np.float32)
@@ -39,7 +39,7 @@ def _setup(albedo, shading):
     return h, t, bary, face, vn
 
 
-def _call(h, t, bary, face, vn, entry, workspace=None):
+def _call(h, t, bary, face, vn, entry, workspace=None, target=True):
     import torch
     from gvr import _lib
     dev = t["vertex_pos"].device
@@ -50,28 +50,52 @@ def _call(h, t, bary, face, vn, entry, workspace=None):
     p = lambda x: None if x is None else ctypes.c_void_p(x.data_ptr())
     args = _lib.GvrBackwardArgs(B, Ht, Wt, p(t["grad_render"]), p(t["vertex_pos"]), p(t["vertex_color"]),
                                 p(t["texture"]), p(t["sh_coeff"]), p(t["target_image"]), p(vn), p(bary), p(face),
-                                p(t["grad_target"]), p(t["extrinsics"]), p(t["intrinsics"]), *[p(o) for o in outs],
-                                p(workspace), 0 if workspace is None else workspace.numel())
+                                p(t["grad_target"]) if target else None, p(t["extrinsics"]), p(t["intrinsics"]),
+                                *[p(o) for o in outs], p(workspace), 0 if workspace is None else workspace.numel())
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     _lib.check(entry(h.ptr, ctypes.byref(args), stream))
     torch.cuda.synchronize()
     return [o.cpu().numpy() for o in outs]
 
 
-@pytest.mark.parametrize("albedo,shading", [("vertexColor", "shaded"), ("textured", "shaded")])
-def test_noalloc_backward_matches_backward(albedo, shading):
+def _same(got, ref):
+    for a, b in zip(got, ref):
+        assert np.isfinite(a).all()
+        if np.all(b == 0):
+            assert np.all(a == 0)
+        else:
+            assert rel_norm(a, b) <= GRAD_TOL
+
+
+# (albedo, shading, batch, target gradient): every part of the scratch is
+# written by at least one case (per-face accumulators and SH partials in
+# the shaded modes, face records in all), and "normal" needs none at all
+CASES = [("vertexColor", "shaded", 1, True), ("textured", "shaded", 1, False), ("vertexColor", "shaded", 2, False),
+         ("textured", "shadeless", 2, True), ("foregroundMask", "shaded", 1, True), ("normal", "shaded", 1, False)]
+
+
+def _reference(case):
     import torch
-    h, t, bary, face, vn = _setup(albedo, shading)
-    ws = torch.empty(h.backward_workspace_size(1), dtype=torch.uint8, device=t["vertex_pos"].device)
-    ref = _call(h, t, bary, face, vn, h._L.gvr_backward, ws)
+    albedo, shading, batch, target = case
+    h, t, bary, face, vn = _setup(albedo, shading, batch)
+    ws = torch.empty(max(h.backward_workspace_size(batch), 256), dtype=torch.uint8, device=t["vertex_pos"].device)
+    return (h, t, bary, face, vn), _call(h, t, bary, face, vn, h._L.gvr_backward, ws, target)
+
+
+@pytest.mark.parametrize("case", CASES, ids=["-".join(map(str, c)) for c in CASES])
+def test_noalloc_backward_matches_backward(case):
+    (h, t, bary, face, vn), ref = _reference(case)
     for _ in range(2):  # the second call starts from the first call's scratch contents
-        got = _call(h, t, bary, face, vn, h._L.gvr_backward_noalloc)
-        for a, b in zip(got, ref):
-            assert np.isfinite(a).all()
-            if np.all(b == 0):
-                assert np.all(a == 0)
-            else:
-                assert rel_norm(a, b) <= GRAD_TOL
+        _same(_call(h, t, bary, face, vn, h._L.gvr_backward_noalloc, target=case[3]), ref)
+
+
+def test_noalloc_calls_of_different_shapes_in_a_row():
+    """Each call starts from whatever the previous call, of another mode or
+    batch size, left in the shared array; results must not depend on it."""
+    runs = [(_reference(c), c[3]) for c in CASES]
+    for _ in range(2):
+        for ((h, t, bary, face, vn), ref), target in runs:
+            _same(_call(h, t, bary, face, vn, h._L.gvr_backward_noalloc, target=target), ref)
 
 
 def test_noalloc_rejects_calls_beyond_its_scratch():
