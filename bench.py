@@ -213,7 +213,7 @@ def run_reference(args):
         o.backward(out["face"], out["bary"], out["vertex_normal"], s["grad_render"][0][sl], s["target_image"][0][sl],
                    s["grad_target"][0][sl])
 
-    for k in range(min(args.warmup, 2)):
+    for k in range(args.warmup):
         one_view(k % s["num_views"])
     times = []
     for k in range(args.steps):
@@ -223,7 +223,7 @@ def run_reference(args):
     ms = 1e3 * sum(times) / len(times)
     value = P1 / (ms / 1e3) / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": min(args.warmup, 2), "ms_per_step": ms, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "batch": 1, "views": 8, "resolution": 1024, "faces": 70000,
                        "vertices": 35002, "texture": 1024, "parallelism": "replicas"},
@@ -231,7 +231,41 @@ def run_reference(args):
                              "sample": "each step: one of the 8 views (cycling) at 1024^2, fwd+bwd, on the CPU "
                                        "oracle (the reference has no CPU path; its kernels are CUDA only)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    gpu = reference_kernels_gpu(s)
+    if gpu is not None:
+        line["reference_kernels_gpu"] = gpu
     print(json.dumps(line), flush=True)
+
+
+def reference_kernels_gpu(s, reps=3):
+    """The reference's own CUDA kernels (cpp/src/Renderer/CUDABasedRasterization{,Grad}.cu,
+    compiled unmodified for sm_103a with nvcc's default flags into
+    oracle/_ref) on the same workload and GPU: mean forward and backward ms
+    of `reps` calls after one warm-up (the reference's kernel timing, CUDA
+    events around its launch sequence).  None where no GPU or no build."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        from oracle import refcore
+        if not refcore.available():
+            return None
+        ref = refcore.Refcore(fmad=True)
+        fwd = ref.forward(s)
+        ref.backward(s, fwd)
+        f_ms, b_ms = [], []
+        for _ in range(reps):
+            fwd = ref.forward(s)
+            f_ms.append(fwd["ms"])
+            b_ms.append(ref.backward(s, fwd)["ms"])
+        ref.close()
+    except Exception as exc:  # a measurement beside the line, never a failure of it
+        return {"unavailable": f"{type(exc).__name__}: {exc}"}
+    P = s["num_views"] * s["width"] * s["height"]
+    f, b = sum(f_ms) / reps, sum(b_ms) / reps
+    return {"fwd_ms": f, "bwd_ms": b, "value": P / ((f + b) / 1e3) / 1e6, "unit": UNIT, "reps": reps,
+            "build": "reference kernels from their sources, nvcc defaults, sm_103a; one GPU, same workload",
+            "gpu": torch.cuda.get_device_name(0)}
 
 
 def run_gvr(args):

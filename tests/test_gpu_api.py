@@ -48,6 +48,32 @@ def test_getters_shapes_and_dtypes():
     assert r.getNormalMap() is None
 
 
+def test_target_image_out_is_a_copy_of_target_image():
+    """Output 4 of the forward op is target_image copied device to device
+    (cpp/src/TensorflowOperators/CudaRenderer/CudaRenderer.cpp:286): equal
+    bytes, in a buffer of its own, for every batch element and view."""
+    import torch
+    from gvr import renderer
+    s = small_scene(views=2, size=48, batch=2)
+    rng = np.random.default_rng(3)
+    s["target_image"] = rng.uniform(-2, 2, s["target_image"].shape).astype(np.float32)
+    s["target_image"][0, 1, 5, 7] = [np.nan, np.inf, -0.0]          # bytes, not values, are copied
+    dev = torch.device("cuda", 0)
+    h = renderer.get_handle(s["faces"], s["uvs"], s["num_vertices"], s["num_views"], s["width"], s["height"],
+                            s["albedo_mode"], s["shading_mode"], device=dev)
+    t = {k: torch.from_numpy(np.ascontiguousarray(s[k])).to(dev)
+         for k in ("vertex_pos", "vertex_color", "texture", "sh_coeff", "extrinsics", "intrinsics", "target_image")}
+    out = renderer.render_forward(h, t["vertex_pos"], t["vertex_color"], t["texture"], t["sh_coeff"],
+                                  t["extrinsics"], t["intrinsics"], target_image=t["target_image"], copy_target=True)
+    torch.cuda.synchronize()
+    tout = out[4]
+    assert tout.data_ptr() != t["target_image"].data_ptr()
+    assert np.array_equal(tout.cpu().numpy().view(np.uint32), s["target_image"].view(np.uint32))
+    # through the operator surface, too
+    r = _renderer(s)
+    assert np.array_equal(r.getTargetBufferTF().cpu().numpy().view(np.uint32), s["target_image"].view(np.uint32))
+
+
 def test_autograd_matches_raw_backward():
     import torch
     from gvr import renderer

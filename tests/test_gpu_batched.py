@@ -134,3 +134,49 @@ def test_plan_refuses_normal_map_handles_and_bad_tiles():
     assert e.value.status == -1
     L = _lib.load()
     assert L.gvr_plan_create(None, 0, 0, ctypes.byref(ctypes.c_void_p())) == -1
+
+
+def test_full_uneven_workload_against_single_calls_and_oracle():
+    """The whole uneven workload of the batched bench (64 displaced spheres,
+    1k..200k faces, 1..8 views at 256/512/1024^2, mixed modes, 512^2
+    textures), autotuned and replayed as a CUDA graph: every job equals
+    gvr_forward bit for bit, and sampled (job, view) pairs -- the densest
+    mesh at its lowest resolution, the largest at its highest, the smallest,
+    and three drawn at random -- equal the FP64 oracle (face ids,
+    barycentrics, vertex normals bit-exact; render 1e-5) given the device's
+    rays."""
+    import torch
+    from gvr import scenes
+    from gvr.batch import BatchPlan
+    from helpers import oracle_scene, rel_max
+    dev = torch.device("cuda", 0)
+    specs = scenes.uneven_batch(seed=0, num_meshes=64)
+    jobs = _plan_jobs(specs, dev)
+    plan = BatchPlan(jobs, autotune=True)
+    stream = torch.cuda.Stream(dev)
+    with torch.cuda.stream(stream):
+        plan.forward(stream=stream, graph=True)
+        plan.forward(stream=stream, graph=True)   # a replay writes the same bits
+    stream.synchronize()
+    _check(plan, jobs)
+    F = [s["faces"].shape[0] for s in specs]
+    R = [s["width"] for s in specs]
+    big = max(F)
+    picks = {min((j for j in range(len(specs)) if F[j] == big), key=lambda j: R[j]),
+             max((j for j in range(len(specs)) if F[j] == big), key=lambda j: R[j]),
+             min(range(len(specs)), key=lambda j: F[j])}
+    rng = np.random.default_rng(5)
+    picks |= set(int(x) for x in rng.choice(len(specs), size=3, replace=False))
+    for j in sorted(picks):
+        s, out, h = specs[j], plan.outputs[j], plan.handles[j]
+        c = int(rng.integers(0, s["num_views"]))
+        rays = h.debug_rays(plan.inputs[j]["extrinsics"], plan.inputs[j]["intrinsics"]).cpu().numpy()[0]
+        one = dict(s, num_views=1, sh_coeff=s["sh_coeff"][:, c:c + 1], extrinsics=s["extrinsics"][:, c:c + 1],
+                   intrinsics=s["intrinsics"][:, c:c + 1])
+        ref = oracle_scene(one, 0, rays=rays[c:c + 1]).forward()
+        face = out["face"].cpu().numpy()[0, c]
+        assert np.array_equal(face, ref["face"][0]), (j, c, int((face != ref["face"][0]).sum()))
+        assert _same(out["barycentric"].cpu().numpy()[0, c], ref["bary"][0]), (j, c)
+        assert _same(out["vertex_normal"].cpu().numpy()[0, c], ref["vertex_normal"][0]), (j, c)
+        assert rel_max(out["render"].cpu().numpy()[0, c], ref["render"][0]) <= 1e-5, (j, c)
+    plan.close()
