@@ -95,35 +95,19 @@ __device__ __forceinline__ void add_texel(float *t, float g0, float g1, float g2
     }
 }
 
-struct BwdIO {
-    const float *grad_render;  // [B,C,H,W,3]
-    const float *verts;        // [B,N,3]
-    const float *colors;       // [B,N,3]
-    const float *texture;      // [B,Ht,Wt,3]
-    const float *sh;           // [B,C,27]
-    const float *target;       // [B,C,H,W,3]
-    const float *vnormal;      // [B,C,N,3]
-    const float *bary_in;      // [B,C,H,W,2] or null
-    const int32_t *face;       // [B,C,H,W]
-    const float *grad_target;  // [B,C,H,W,3] or null
-    float *tex_grad;           // [B,Ht,Wt,3]
-    int imageFilter;
-    int phong;                 // GVR_SHADING_PHONG: albedo scaled by the headlight term, no SH
-};
-
 // ALBPOS (vertexColor only, opt-in): add the change of the interpolated
 // vertex colour through the barycentrics to the position gradient, which the
 // reference leaves out (CUDABasedRasterizationGrad.cu:489).
 template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
-__global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
-                                                         const BwdIO io) {
+__device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &dims, const BwdScratch &ws,
+                                         const BwdIO &io, const int item) {
     constexpr bool COL = MODE == GVR_ALBEDO_VERTEX_COLOR;
     constexpr bool POS = SHADED || TARGET || ALBPOS;
     constexpr int NPOS = POS ? 9 : 0, NGN = SHADED ? 9 : 0, NCOL = COL ? 9 : 0;
     constexpr int NV = NPOS + NGN + NCOL > 0 ? NPOS + NGN + NCOL : 1;
 
     const int T = dims.tilesX * dims.tilesY;
-    const int tile = blockIdx.x % T, bc = blockIdx.x / T, b = bc / dims.C;
+    const int tile = item % T, bc = item / T, b = bc / dims.C;
     const int tileX0 = (tile % dims.tilesX) * kTile, tileY0 = (tile / dims.tilesX) * kTile;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int u = tileX0 + (tid & (kTile - 1)), v = tileY0 + tid / kTile;
@@ -426,6 +410,13 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo,
             ws.shPartial[((size_t)bc * T + tile) * 27 + tid] = s;
         }
     }
+}
+
+// One block per 16 x 16 tile of one call.
+template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
+__global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
+                                                         const BwdIO io) {
+    bwd_tile<MODE, SHADED, TARGET, ALBPOS>(topo, dims, ws, io, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------- vertex gathers

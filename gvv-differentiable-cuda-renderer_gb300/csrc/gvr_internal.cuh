@@ -366,4 +366,21 @@ struct BwdScratch {
     float *shPartial;    // [B*C*T*27]
 };
 
+// Inputs and outputs of the backward's pixel kernel.
+struct BwdIO {
+    const float *grad_render;  // [B,C,H,W,3]
+    const float *verts;        // [B,N,3]
+    const float *colors;       // [B,N,3]
+    const float *texture;      // [B,Ht,Wt,3]
+    const float *sh;           // [B,C,27]
+    const float *target;       // [B,C,H,W,3]
+    const float *vnormal;      // [B,C,N,3]
+    const float *bary_in;      // [B,C,H,W,2] or null
+    const int32_t *face;       // [B,C,H,W]
+    const float *grad_target;  // [B,C,H,W,3] or null
+    float *tex_grad;           // [B,Ht,Wt,3]
+    int imageFilter;
+    int phong;                 // GVR_SHADING_PHONG: albedo scaled by the headlight term, no SH
+};
+
 }  // namespace gvr

@@ -212,7 +212,7 @@ def _fixture_scene(name, albedo, shading, batch, seed):
         pytest.skip(f"scene {name} not built (oracle/_ref/scene_{name}.npz; needs the reference's data files)")
     C, (H, W) = sc["extrinsics"].shape[0], (int(x) for x in sc["size"])
     rng = np.random.default_rng(seed)
-    rep = lambda a: np.ascontiguousarray(np.broadcast_to(a[None], (batch,) + a.shape), np.float32)
+    rep = lambda a: np.repeat(np.asarray(a, np.float32)[None], batch, axis=0)
     sh = rep(sc["sh_coeff"])
     sh[1:] += rng.uniform(0, 0.5, sh[1:].shape).astype(np.float32)
     return dict(faces=sc["faces"], uvs=sc["uvs"], num_vertices=sc["vertex_pos"].shape[0], num_views=C, width=W,
