@@ -34,7 +34,7 @@ namespace {
 
 constexpr int kChunk = kTilePix;  // face entries staged per pass: one per thread
 constexpr int kBuckets = 128;     // depth buckets of the front-to-back order
-constexpr int kMaxCand = 7;       // candidates a pixel keeps in registers
+constexpr int kMaxCand = 8;       // candidates a pixel keeps (shared-memory slots per pixel)
 
 // Face entry with its skip-test constants and its box clipped to the tile
 // (80 bytes).  Fields are grouped in 16-byte rows in the order the walk
@@ -56,9 +56,11 @@ __device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX
     E.b1 = vf.s1.y;
     E.a2 = vf.s1.z;
     E.b2 = vf.s1.w;
-    E.r0 = __frcp_rn(vf.z.x);
-    E.r1 = __frcp_rn(vf.z.y);
-    E.r2 = __frcp_rn(vf.z.z);
+    // reciprocal depths feed only the depth estimate of the skip tests, whose
+    // margin dRel is orders of magnitude above this approximation's error
+    E.r0 = __fdividef(1.0f, vf.z.x);
+    E.r1 = __fdividef(1.0f, vf.z.y);
+    E.r2 = __fdividef(1.0f, vf.z.z);
     E.mIn = vf.z.w;
     E.mOut = vf.s0.z;
     E.dRel = vf_drel(vf);
@@ -191,17 +193,15 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     // The tile's entries go through shared memory in chunks of kChunk (dense
     // meshes at low resolution put thousands of faces in a tile); zup and
     // the candidates carry over from chunk to chunk.
+    // Candidates live in shared memory, slot j of pixel tid at [j][tid]
+    // (conflict-free): appending is two stores, and the resolve walks them
+    // with one copy of the exact test instead of one per register slot.
+    __shared__ int sCandF[kMaxCand][kTilePix];
+    __shared__ float sCandZ[kMaxCand][kTilePix];
     float zup = kInf;
     int nLast = 0;  // kept entries of the last chunk (all of them when nAll <= kChunk)
     int nCand = 0;
     bool spill = false;
-    int cf[kMaxCand];
-    float cz[kMaxCand];
-#pragma unroll
-    for (int j = 0; j < kMaxCand; ++j) {
-        cf[j] = -1;
-        cz[j] = kInf;
-    }
     // The view's range of finite, non-negative depth bounds, from the binning
     // pass: every kept entry with such a bound lies in it.
     const unsigned zr0 = ws.zRange[2 * bc], zr1 = ws.zRange[2 * bc + 1];
@@ -325,16 +325,14 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             }
             if (nCand == kMaxCand) {  // make room: drop candidates now known to lose
                 int m = 0;
-#pragma unroll
+#pragma unroll 1
                 for (int j = 0; j < kMaxCand; ++j) {
-                    const bool keepC = !(cz[j] > zup);
-#pragma unroll
-                    for (int t = 0; t < kMaxCand; ++t)
-                        if (keepC && t == m) {
-                            cf[t] = cf[j];
-                            cz[t] = cz[j];
-                        }
-                    m += keepC;
+                    const float zj = sCandZ[j][tid];
+                    if (!(zj > zup)) {
+                        sCandF[m][tid] = sCandF[j][tid];
+                        sCandZ[m][tid] = zj;
+                        ++m;
+                    }
                 }
                 nCand = m;
             }
@@ -342,13 +340,8 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
                 spill = true;
                 continue;
             }
-            const int fE = __float_as_int(h.w);
-#pragma unroll
-            for (int t = 0; t < kMaxCand; ++t)
-                if (t == nCand) {
-                    cf[t] = fE;
-                    cz[t] = zlow;
-                }
+            sCandF[nCand][tid] = __float_as_int(h.w);
+            sCandZ[nCand][tid] = zlow;
             ++nCand;
             }  // entries of the group that meet the block
         }
@@ -366,14 +359,16 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     unsigned long long best = kEmptyKey;
     V3 abc = v3(0.0f, 0.0f, 0.0f);
     if (!spill) {
+        // the live candidates (bound not above the final zup) first, so that
+        // the warp's exact tests line up: pass j tests every pixel's j-th
         int nLive = 0;
-#pragma unroll
-        for (int j = 0; j < kMaxCand; ++j) nLive += (j < nCand && !(cz[j] > zup));
-#pragma unroll
-        for (int j = 0; j < kMaxCand; ++j) {
-            if (j >= nCand || cz[j] > zup) continue;
+#pragma unroll 1
+        for (int j = 0; j < nCand; ++j)
+            if (!(sCandZ[j][tid] > zup)) sCandF[nLive++][tid] = sCandF[j][tid];
+#pragma unroll 1
+        for (int j = 0; j < nLive; ++j) {
             V3 t;
-            const unsigned long long k = exact_key(x, cf[j], t, nLive > 1);
+            const unsigned long long k = exact_key(x, sCandF[j][tid], t, nLive > 1);
             if (k < best) {
                 best = k;
                 abc = t;
