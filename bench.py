@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--views", type=int, default=8, help="views of the workload (profiling runs use fewer)")
     ap.add_argument("--workload", choices=["multiview", "batched", "fit", "learned"], default="multiview",
                     help="multiview: the fwd+bwd step above (default); batched: 64 uneven meshes through one "
-                         "plan (forward), against the same jobs as one gvr_forward call each; fit: plain "
+                         "plan (forward + backward), against the same jobs as one call each; fit: plain "
                          "analysis-by-synthesis fits of the morphable model; learned: train the proposal "
                          "network, then fit from its proposals against the plain fit")
     ap.add_argument("--meshes", type=int, default=64, help="meshes of the batched workload")
@@ -490,10 +490,12 @@ def run_gvr(args):
 def run_batched(args):
     """Uneven batch: `--meshes` displaced spheres with 1k..200k faces, 1..8
     views each at 256^2/512^2/1024^2, mixed modes, 512^2 textures (views of a
-    mesh sharing a resolution form one job).  One step = the forward of every
-    job.  Timed three ways on the same buffers: the plan replayed as a CUDA
-    graph (autotuned tiles; the value), the plan launched eagerly, and one
-    gvr_forward call per job (the per-mesh loop)."""
+    mesh sharing a resolution form one job).  One step = the forward and the
+    backward (upstream gradients N(0, 1)) of every job.  Timed three ways on
+    the same buffers: the plan's forward and backward replayed as CUDA graphs
+    (autotuned tiles; the value), the plan launched eagerly, and one
+    gvr_forward + gvr_backward call per job (the per-mesh loop); the
+    forward alone is reported beside them."""
     import torch
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
@@ -534,13 +536,36 @@ def run_batched(args):
                 total += e0.elapsed_time(e1)
         return reduce_max(total / args.steps, world)
 
+    # upstream gradients N(0, 1) for every job, bound once (the buffers stay)
+    import numpy as np
+    rng = np.random.default_rng(rank)
+    plan.forward(stream=stream)
+    plan.bind_backward([rng.normal(0, 1, (1, s["num_views"], s["height"], s["width"], 3)).astype(np.float32)
+                        for s in specs])
+    stream.synchronize()
+
+    def graph_step():
+        plan.forward(stream=stream, graph=True)
+        plan.backward(stream=stream, graph=True)
+
+    def eager_step():
+        plan.forward(stream=stream)
+        plan.backward(stream=stream)
+
+    def per_call_step():
+        plan.forward_per_call(stream=stream)
+        plan.backward_per_call(stream=stream)
+
+    reps = max(3, args.warmup) + args.steps
+    graph_ms = timed(graph_step)
     n0 = L.gvr_launch_count()
-    graph_ms = timed(lambda: plan.forward(stream=stream, graph=True))
-    eager_ms = timed(lambda: plan.forward(stream=stream))
+    eager_ms = timed(eager_step)
     n1 = L.gvr_launch_count()
-    per_call_ms = timed(lambda: plan.forward_per_call(stream=stream))
-    per_call_launches = (L.gvr_launch_count() - n1) / (max(3, args.warmup) + args.steps)
-    eager_launches = (n1 - n0) / (max(3, args.warmup) + args.steps)  # graph replays add none here
+    per_call_ms = timed(per_call_step)
+    per_call_launches = (L.gvr_launch_count() - n1) / reps
+    eager_launches = (n1 - n0) / reps  # graph replays add none here
+    fwd_graph_ms = timed(lambda: plan.forward(stream=stream, graph=True))
+    fwd_per_call_ms = timed(lambda: plan.forward_per_call(stream=stream))
     cfgs = {}
     for j in range(len(jobs)):
         cfgs.setdefault("%dx%d/%d" % plan.tile_config(j), 0)
@@ -548,7 +573,7 @@ def run_batched(args):
     if rank != 0:
         return
     value = world * P / (graph_ms / 1e3) / 1e6
-    line = {"metric": "batched fwd Mpix/s (64 uneven meshes)", "value": value, "unit": UNIT, "n_gpus": world,
+    line = {"metric": "batched fwd+bwd Mpix/s (64 uneven meshes)", "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": graph_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
             "config": {"workload": f"uneven_batch: {args.meshes} displaced spheres, faces log-uniform 1k..200k, "
@@ -559,6 +584,8 @@ def run_batched(args):
             "faces_per_s": world * faces / (graph_ms / 1e3),
             "plan_graph_ms": graph_ms, "plan_eager_ms": eager_ms, "per_call_ms": per_call_ms,
             "per_call_mpix_s": P / (per_call_ms / 1e3) / 1e6,
+            "forward_only": {"plan_graph_ms": fwd_graph_ms, "per_call_ms": fwd_per_call_ms,
+                             "plan_graph_mpix_s": P / (fwd_graph_ms / 1e3) / 1e6},
             "launches_per_step": {"plan": eager_launches, "per_call": per_call_launches},
             "autotune_s": tune_s, "tile_configs": cfgs}
     print(json.dumps(line), flush=True)

@@ -382,7 +382,9 @@ int gvr_forward(GvrHandle *h, const GvrForwardArgs *a, void *stream) {
     return forward_epilogue(h, a, st);
 }
 
-int gvr_backward(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
+// Checks the backward arguments against the handle (shared by the per-call
+// and the batched backward).
+static int check_backward_args(const GvrHandle *h, const GvrBackwardArgs *a) {
     if (!h || !a) return fail(GVR_ERR_INVALID_ARGUMENT, "handle/args is NULL");
     const int B = a->batch;
     if (!batch_fits(h, B)) return fail(GVR_ERR_INVALID_ARGUMENT, "batch must be >= 1 and the call within int32 index range");
@@ -403,12 +405,25 @@ int gvr_backward(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
         if (a->target_grad && !a->target_image)
             return fail(GVR_ERR_INVALID_ARGUMENT, "target_grad needs target_image");
     }
+    return GVR_OK;
+}
+
+static bool zero_gradient_mode(const GvrHandle *h) {
+    const int mode = h->attrs.albedo_mode;
+    return mode == GVR_ALBEDO_NORMAL || mode == GVR_ALBEDO_LIGHTING || mode == GVR_ALBEDO_UV;
+}
+
+int gvr_backward(GvrHandle *h, const GvrBackwardArgs *a, void *stream) {
+    int rc = check_backward_args(h, a);
+    if (rc != GVR_OK) return rc;
+    const int B = a->batch;
+    const bool zeroMode = zero_gradient_mode(h);
     DeviceGuard g(h->device);
     if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CallScratch scratch;
     if (!zeroMode) {
-        int rc = scratch.acquire(a->workspace, a->workspace_bytes, bwd_layout(h, B, nullptr).bytes, st);
+        rc = scratch.acquire(a->workspace, a->workspace_bytes, bwd_layout(h, B, nullptr).bytes, st);
         if (rc != GVR_OK) return rc;
     }
     BwdLayout L = bwd_layout(h, B, scratch.ptr);
@@ -487,6 +502,20 @@ extern "C" int gvr_backward_noalloc(GvrHandle *h, const GvrBackwardArgs *a, void
 
 // ---------------------------------------------------------------------------- batched forward plans
 
+// The backward half of a plan (gvr_plan_bind_backward): one backward call per job.
+struct PlanBackward {
+    std::vector<GvrBackwardArgs> args;
+    void *d_mem = nullptr;  // every job's scratch and the tables
+    gvr::BwdBatchLaunch launch{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~PlanBackward() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (d_mem) cudaFree(d_mem);
+    }
+};
+
 struct GvrPlan {
     int device = 0;
     std::vector<GvrJob> jobs;
@@ -495,6 +524,7 @@ struct GvrPlan {
     gvr::BatchLaunch launch{};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    PlanBackward *bwd = nullptr;
 };
 
 namespace {
@@ -775,9 +805,219 @@ int gvr_plan_tile_config(const GvrPlan *p, int32_t job, int32_t *tile_w, int32_t
     return GVR_OK;
 }
 
+int gvr_plan_bind_backward(GvrPlan *p, const GvrBackwardArgs *args, int32_t count) {
+    if (!p) return fail(GVR_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!args || count != (int)p->jobs.size())
+        return fail(GVR_ERR_INVALID_ARGUMENT, "one backward call per job of the plan, in the plan's job order");
+    for (int j = 0; j < count; ++j) {
+        const int rc = check_backward_args(p->jobs[j].handle, &args[j]);
+        if (rc != GVR_OK) return fail(rc, "job " + std::to_string(j) + ": " + g_error);
+    }
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    using gvr::BwdBatchLaunch;
+    const int J = count;
+    // host tables: per-stage block offsets, clearing regions and pixel groups
+    std::vector<int> start[gvr::kNumBwdStages];
+    for (auto &v : start) v.assign(J + 1, 0);
+    long long total[gvr::kNumBwdStages] = {0};
+    std::vector<int> variant(J);
+    std::vector<std::vector<int>> groupJobs(gvr::kNumBwdVariants), groupStart(gvr::kNumBwdVariants);
+    std::vector<long long> groupTotal(gvr::kNumBwdVariants, 0);
+    for (int j = 0; j < J; ++j) {
+        const GvrHandle *h = p->jobs[j].handle;
+        const GvrBackwardArgs &a = args[j];
+        const long long B = a.batch, C = h->attrs.num_cameras;
+        variant[j] = gvr::backward_variant(h->attrs.albedo_mode, h->attrs.shading_mode, a.target_grad != nullptr,
+                                           (a.flags & GVR_BACKWARD_ALBEDO_POSITION) != 0);
+        const bool zero = variant[j] < 0;
+        const long long n[gvr::kNumBwdStages] = {zero ? 0 : (B * C + gvr::kBatchBlock - 1) / gvr::kBatchBlock,
+                                                 zero ? 0 : (B * h->F + gvr::kBatchBlock - 1) / gvr::kBatchBlock,
+                                                 zero ? 0 : (B * h->N + 255) / 256, zero ? 0 : B * C * 27};
+        for (int st = 0; st < gvr::kNumBwdStages; ++st) {
+            start[st][j] = (int)total[st];
+            total[st] += n[st];
+        }
+        if (!zero) {
+            groupJobs[variant[j]].push_back(j);
+            groupStart[variant[j]].push_back((int)groupTotal[variant[j]]);
+            groupTotal[variant[j]] += B * C * h->tilesX * h->tilesY;
+        }
+    }
+    for (int st = 0; st < gvr::kNumBwdStages; ++st) {
+        if (total[st] >= INT_MAX) return fail(GVR_ERR_INVALID_ARGUMENT, "plan too large for int32 indexing");
+        start[st][J] = (int)total[st];
+    }
+    for (int v = 0; v < gvr::kNumBwdVariants; ++v) {
+        if (groupTotal[v] >= INT_MAX) return fail(GVR_ERR_INVALID_ARGUMENT, "plan too large for int32 indexing");
+        groupStart[v].push_back((int)groupTotal[v]);
+    }
+    // device memory: every job's scratch, then the tables
+    auto measure = [&](void *base, std::vector<BwdLayout> &lay, gvr::BwdJob *&djobs, int *(&dstart)[gvr::kNumBwdStages],
+                       gvr::ZeroRegion *&dzero, int *&dzeroStart, int *&dgroups, size_t nZero, size_t nGroupInts) {
+        Carver c(base);
+        lay.assign(J, BwdLayout{});
+        for (int j = 0; j < J; ++j) {
+            if (variant[j] < 0) continue;
+            Carver sub(base ? static_cast<char *>(base) + ((c.off + 255) & ~size_t(255)) : nullptr);
+            const size_t bytes = bwd_layout(p->jobs[j].handle, args[j].batch, nullptr).bytes;
+            lay[j] = bwd_layout(p->jobs[j].handle, args[j].batch, sub.base);
+            c.take<char>(bytes);
+        }
+        djobs = c.take<gvr::BwdJob>(J);
+        for (int st = 0; st < gvr::kNumBwdStages; ++st) dstart[st] = c.take<int>(J + 1);
+        dzero = c.take<gvr::ZeroRegion>(nZero > 0 ? nZero : 1);
+        dzeroStart = c.take<int>(nZero + 1);
+        dgroups = c.take<int>(nGroupInts > 0 ? nGroupInts : 1);
+        return c.off + 256;
+    };
+    std::vector<BwdLayout> lay;
+    gvr::BwdJob *djobs = nullptr;
+    int *dstart[gvr::kNumBwdStages] = {nullptr};
+    gvr::ZeroRegion *dzero = nullptr;
+    int *dzeroStart = nullptr, *dgroups = nullptr;
+    size_t nZero = 0, nGroupInts = 0;
+    for (int j = 0; j < J; ++j) nZero += variant[j] < 0 ? 4 : 2;
+    for (int v = 0; v < gvr::kNumBwdVariants; ++v)
+        if (!groupJobs[v].empty()) nGroupInts += 2 * groupJobs[v].size() + 1;
+    const size_t bytes = measure(nullptr, lay, djobs, dstart, dzero, dzeroStart, dgroups, nZero, nGroupInts);
+    PlanBackward *b = new PlanBackward();
+    cudaError_t e = cudaMalloc(&b->d_mem, bytes);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "cudaMalloc(plan backward)");
+    }
+    measure(b->d_mem, lay, djobs, dstart, dzero, dzeroStart, dgroups, nZero, nGroupInts);
+    // host copies of the job records, clearing regions and groups
+    std::vector<gvr::BwdJob> hostJobs(J);
+    std::vector<gvr::ZeroRegion> zeros;
+    std::vector<int> zeroStart(1, 0);
+    auto addZero = [&](void *ptr, long long floats) {
+        zeros.push_back(gvr::ZeroRegion{static_cast<float *>(ptr), floats});
+        zeroStart.push_back(zeroStart.back() + (int)((floats + gvr::kZeroPerBlock - 1) / gvr::kZeroPerBlock));
+    };
+    for (int j = 0; j < J; ++j) {
+        const GvrHandle *h = p->jobs[j].handle;
+        const GvrBackwardArgs &a = args[j];
+        const long long B = a.batch, C = h->attrs.num_cameras;
+        gvr::BwdJob &R = hostJobs[j];
+        std::memset(&R, 0, sizeof(R));
+        R.topo = h->topo();
+        R.dims = dims_of(h, a.batch, a.texture_height, a.texture_width);
+        R.ws = lay[j].s;
+        const int phong = h->attrs.shading_mode == GVR_SHADING_PHONG && h->attrs.albedo_mode != GVR_ALBEDO_FOREGROUND_MASK;
+        R.io = gvr::BwdIO{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image,
+                          a.vertex_normal, a.barycentric, a.face, a.target_grad, a.texture_grad,
+                          h->attrs.image_filter_size, phong};
+        R.extr = a.extrinsics;
+        R.intr = a.intrinsics;
+        R.vpos_grad = a.vertex_pos_grad;
+        R.vcol_grad = a.vertex_color_grad;
+        R.sh_grad = a.sh_coeff_grad;
+        R.zeroMode = variant[j] < 0;
+        R.shaded = h->attrs.shading_mode == GVR_SHADING_SHADED && h->attrs.albedo_mode != GVR_ALBEDO_FOREGROUND_MASK;
+        R.useCol = h->attrs.albedo_mode == GVR_ALBEDO_VERTEX_COLOR;
+        const long long tex = B * a.texture_height * a.texture_width * 3;
+        if (R.zeroMode) {
+            addZero(a.vertex_pos_grad, B * h->N * 3);
+            addZero(a.vertex_color_grad, B * h->N * 3);
+            addZero(a.texture_grad, tex);
+            addZero(a.sh_coeff_grad, B * C * 27);
+        } else {
+            addZero(R.ws.faceAcc, B * h->F * gvr::kFaceAccFloats);
+            addZero(a.texture_grad, tex);
+        }
+    }
+    std::vector<int> groupInts;
+    gvr::BwdBatchLaunch &L = b->launch;
+    L.nGroups = 0;
+    for (int v = 0; v < gvr::kNumBwdVariants; ++v) {
+        if (groupJobs[v].empty()) continue;
+        const int g = L.nGroups++;
+        L.groupVariant[g] = v;
+        L.groupCount[g] = (int)groupJobs[v].size();
+        L.groupBlocks[g] = groupStart[v].back();
+        L.groupJobs[g] = dgroups + groupInts.size();
+        groupInts.insert(groupInts.end(), groupJobs[v].begin(), groupJobs[v].end());
+        L.groupStart[g] = dgroups + groupInts.size();
+        groupInts.insert(groupInts.end(), groupStart[v].begin(), groupStart[v].end());
+    }
+    e = cudaMemcpy(djobs, hostJobs.data(), sizeof(gvr::BwdJob) * J, cudaMemcpyHostToDevice);
+    for (int st = 0; st < gvr::kNumBwdStages && e == cudaSuccess; ++st)
+        e = cudaMemcpy(dstart[st], start[st].data(), sizeof(int) * (J + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !zeros.empty())
+        e = cudaMemcpy(dzero, zeros.data(), sizeof(gvr::ZeroRegion) * zeros.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dzeroStart, zeroStart.data(), sizeof(int) * zeroStart.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !groupInts.empty())
+        e = cudaMemcpy(dgroups, groupInts.data(), sizeof(int) * groupInts.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "plan backward setup");
+    }
+    if (zeroStart.back() >= INT_MAX) {
+        delete b;
+        return fail(GVR_ERR_INVALID_ARGUMENT, "plan too large for int32 indexing");
+    }
+    L.jobs = djobs;
+    for (int st = 0; st < gvr::kNumBwdStages; ++st) {
+        L.blockStart[st] = dstart[st];
+        L.blocks[st] = (int)total[st];
+    }
+    L.zeros = dzero;
+    L.zeroStart = dzeroStart;
+    L.nZero = (int)zeros.size();
+    L.zeroBlocks = zeroStart.back();
+    L.nJobs = J;
+    b->args.assign(args, args + count);
+    delete p->bwd;
+    p->bwd = b;
+    return GVR_OK;
+}
+
+int gvr_plan_backward(GvrPlan *p, void *stream) {
+    if (!p) return fail(GVR_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!p->bwd) return fail(GVR_ERR_INVALID_ARGUMENT, "no backward bound to the plan (gvr_plan_bind_backward)");
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    const cudaError_t e = gvr::launch_backward_batched(p->bwd->launch, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? GVR_OK : cuda_fail(e, "batched backward launch");
+}
+
+int gvr_plan_backward_graph(GvrPlan *p, void *stream) {
+    if (!p) return fail(GVR_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (!p->bwd) return fail(GVR_ERR_INVALID_ARGUMENT, "no backward bound to the plan (gvr_plan_bind_backward)");
+    if (!stream) return fail(GVR_ERR_INVALID_ARGUMENT, "graph capture needs a created (non-default) stream");
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    PlanBackward *b = p->bwd;
+    if (!b->exec) {
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+        const cudaError_t le = gvr::launch_backward_batched(b->launch, st);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(st, &graph);
+        if (le != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return cuda_fail(le, "batched backward launch");
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->exec, graph, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            b->exec = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+        b->graph = graph;
+    }
+    const cudaError_t e = cudaGraphLaunch(b->exec, st);
+    return e == cudaSuccess ? GVR_OK : cuda_fail(e, "cudaGraphLaunch");
+}
+
 void gvr_plan_destroy(GvrPlan *p) {
     if (!p) return;
     DeviceGuard g(p->device);
+    delete p->bwd;
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->d_mem) cudaFree(p->d_mem);

@@ -98,17 +98,18 @@ __device__ __forceinline__ void add_texel(float *t, float g0, float g1, float g2
 // ALBPOS (vertexColor only, opt-in): add the change of the interpolated
 // vertex colour through the barycentrics to the position gradient, which the
 // reference leaves out (CUDABasedRasterizationGrad.cu:489).
+// Tile (tx, ty) of view bc (= batch * C + camera).
 template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
 __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &dims, const BwdScratch &ws,
-                                         const BwdIO &io, const int item) {
+                                         const BwdIO &io, const int bc, const int tx, const int ty) {
     constexpr bool COL = MODE == GVR_ALBEDO_VERTEX_COLOR;
     constexpr bool POS = SHADED || TARGET || ALBPOS;
     constexpr int NPOS = POS ? 9 : 0, NGN = SHADED ? 9 : 0, NCOL = COL ? 9 : 0;
     constexpr int NV = NPOS + NGN + NCOL > 0 ? NPOS + NGN + NCOL : 1;
 
     const int T = dims.tilesX * dims.tilesY;
-    const int tile = item % T, bc = item / T, b = bc / dims.C;
-    const int tileX0 = (tile % dims.tilesX) * kTile, tileY0 = (tile / dims.tilesX) * kTile;
+    const int tile = ty * dims.tilesX + tx, b = bc / dims.C;
+    const int tileX0 = tx * kTile, tileY0 = ty * kTile;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int u = tileX0 + (tid & (kTile - 1)), v = tileY0 + tid / kTile;
     const bool inImage = u < dims.W && v < dims.H;
@@ -412,22 +413,47 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
     }
 }
 
-// One block per 16 x 16 tile of one call.
+// One block per 16 x 16 tile of one call: grid (tilesX, tilesY, views),
+// views bcBase .. bcBase + gridDim.z - 1.
 template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
 __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
-                                                         const BwdIO io) {
-    bwd_tile<MODE, SHADED, TARGET, ALBPOS>(topo, dims, ws, io, blockIdx.x);
+                                                         const BwdIO io, int bcBase) {
+    bwd_tile<MODE, SHADED, TARGET, ALBPOS>(topo, dims, ws, io, bcBase + blockIdx.z, blockIdx.x, blockIdx.y);
+}
+
+// One block per 16 x 16 tile of every job of one variant in a batched plan:
+// jobList[g] is the g-th job of the variant, its tiles start at block
+// blockStart[g].  The job record is staged in shared memory once per block.
+template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
+__global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels_batched(const BwdJob *__restrict__ jobs,
+                                                                 const int *__restrict__ jobList,
+                                                                 const int *__restrict__ blockStart, int nJobs) {
+    __shared__ BwdJob sJ;
+    __shared__ int sBC, sTX, sTY;
+    const int g = job_of_block(blockStart, nJobs, blockIdx.x);
+    const BwdJob *J = jobs + jobList[g];
+    constexpr int kWords = (int)(sizeof(BwdJob) / sizeof(int));
+    for (int w = threadIdx.x; w < kWords; w += blockDim.x)
+        reinterpret_cast<int *>(&sJ)[w] = reinterpret_cast<const int *>(J)[w];
+    if (threadIdx.x == 0) {  // (view, tile) of the block, decomposed once
+        const int local = blockIdx.x - blockStart[g], tilesX = J->dims.tilesX, T = tilesX * J->dims.tilesY;
+        const int tile = local % T;
+        sBC = local / T;
+        sTX = tile % tilesX;
+        sTY = tile / tilesX;
+    }
+    __syncthreads();
+    bwd_tile<MODE, SHADED, TARGET, ALBPOS>(sJ.topo, sJ.dims, sJ.ws, sJ.io, sBC, sTX, sTY);
 }
 
 // ---------------------------------------------------------------------------- vertex gathers
 
 // Face-accumulator layout (floats): [0..8] position grad of corners 0..2,
 // [9..17] vertex-normal grad of corners 0..2, [20..28] colour grad of corners 0..2.
-__global__ void k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc, float *__restrict__ vpos_grad,
-                           float *__restrict__ vcol_grad, float4 *__restrict__ gN, int useCol, int useGN) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void gather_a_item(const Topology &topo, const float *__restrict__ faceAcc,
+                                              float *__restrict__ vpos_grad, float *__restrict__ vcol_grad,
+                                              float4 *__restrict__ gN, int useCol, int useGN, int i) {
     const int N = topo.N, F = topo.F;
-    if (i >= B * N) return;
     int b = i / N, v = i - b * N;
     float pos[3] = {0, 0, 0}, gn[3] = {0, 0, 0}, col[3] = {0, 0, 0};
     for (int k = topo.vstart[v]; k < topo.vstart[v + 1]; ++k) {
@@ -452,11 +478,15 @@ __global__ void k_gather_a(const Topology topo, int B, const float *__restrict__
     if (useGN) gN[i] = make_float4(gn[0], gn[1], gn[2], 0.0f);
 }
 
-__global__ void k_gather_b(const Topology topo, int B, const float *__restrict__ verts, const float4 *__restrict__ gN,
-                           float *__restrict__ vpos_grad) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc, float *__restrict__ vpos_grad,
+                           float *__restrict__ vcol_grad, float4 *__restrict__ gN, int useCol, int useGN) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < B * topo.N) gather_a_item(topo, faceAcc, vpos_grad, vcol_grad, gN, useCol, useGN, i);
+}
+
+__device__ __forceinline__ void gather_b_item(const Topology &topo, const float *__restrict__ verts,
+                                              const float4 *__restrict__ gN, float *__restrict__ vpos_grad, int i) {
     const int N = topo.N;
-    if (i >= B * N) return;
     int b = i / N, v = i - b * N;
     const float *V = verts + (size_t)b * N * 3;
     const float4 *g = gN + (size_t)b * N;
@@ -481,13 +511,34 @@ __global__ void k_gather_b(const Topology topo, int B, const float *__restrict__
     for (int a = 0; a < 3; ++a) vpos_grad[3 * (size_t)i + a] += acc[a];
 }
 
+__global__ void k_gather_b(const Topology topo, int B, const float *__restrict__ verts, const float4 *__restrict__ gN,
+                           float *__restrict__ vpos_grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < B * topo.N) gather_b_item(topo, verts, gN, vpos_grad, i);
+}
+
+// Both gathers over every job of a batched plan (WHICH 0: gather_a, 1: gather_b).
+template <int WHICH>
+__global__ void __launch_bounds__(256) k_gather_batched(const BwdJob *__restrict__ jobs,
+                                                        const int *__restrict__ blockStart, int nJobs) {
+    const int j = job_of_block(blockStart, nJobs, blockIdx.x);
+    const BwdJob &J = jobs[j];
+    const int i = (blockIdx.x - blockStart[j]) * 256 + threadIdx.x;
+    if (J.zeroMode || i >= J.dims.B * J.topo.N) return;
+    if (WHICH == 0)
+        gather_a_item(J.topo, reinterpret_cast<const float *>(J.ws.faceAcc), J.vpos_grad, J.vcol_grad, J.ws.gN,
+                      J.useCol, J.shaded, i);
+    else if (J.shaded)
+        gather_b_item(J.topo, J.io.verts, J.ws.gN, J.vpos_grad, i);
+}
+
 // One block per (batch, view, coefficient): thread i sums tiles i, i+256, ...
 // (FP32 with compensation), then a fixed-order FP64 tree finishes, so the
 // result is deterministic and FP64-accurate at FP32 cost.
-__global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
-                                                     int tilesPerView, int shaded) {
+__device__ __forceinline__ void sh_finalize_block(const float *__restrict__ partial, float *__restrict__ sh_grad,
+                                                  int tilesPerView, int shaded, int blk) {
     __shared__ double red[256];
-    const int bc = blockIdx.x / 27, k = blockIdx.x % 27;
+    const int bc = blk / 27, k = blk % 27;
     float s = 0.0f, comp = 0.0f;
     if (shaded)
         for (int t = threadIdx.x; t < tilesPerView; t += 256) {
@@ -505,35 +556,115 @@ __global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ p
     if (threadIdx.x == 0) sh_grad[(size_t)bc * 27 + k] = (float)red[0];
 }
 
+__global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
+                                                     int tilesPerView, int shaded) {
+    sh_finalize_block(partial, sh_grad, tilesPerView, shaded, blockIdx.x);
+}
+
+// One block per (job, batch, view, coefficient) of a batched plan.
+__global__ void __launch_bounds__(256) k_sh_finalize_batched(const BwdJob *__restrict__ jobs,
+                                                             const int *__restrict__ blockStart, int nJobs) {
+    const int j = job_of_block(blockStart, nJobs, blockIdx.x);
+    const BwdJob &J = jobs[j];
+    if (J.zeroMode) return;
+    sh_finalize_block(J.ws.shPartial, J.sh_grad, J.dims.tilesX * J.dims.tilesY, J.shaded, blockIdx.x - blockStart[j]);
+}
+
+// Clears every region of a batched backward: region r owns blocks
+// [zeroStart[r], zeroStart[r + 1]), each clearing kZeroPerBlock floats.
+__global__ void __launch_bounds__(256) k_zero_regions(const ZeroRegion *__restrict__ regions,
+                                                      const int *__restrict__ zeroStart, int nRegions) {
+    const int r = job_of_block(zeroStart, nRegions, blockIdx.x);
+    const ZeroRegion R = regions[r];
+    const long long base = (long long)(blockIdx.x - zeroStart[r]) * kZeroPerBlock;
+    for (int k = threadIdx.x; k < kZeroPerBlock; k += 256) {
+        const long long i = base + k;
+        if (i < R.count) R.ptr[i] = 0.0f;
+    }
+}
+
 // ---------------------------------------------------------------------------- host launch
 
 static inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
 
-template <int MODE, bool SHADED, bool TARGET, bool ALBPOS>
-static cudaError_t launch_pixels_t(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const BwdIO &io,
-                                   cudaStream_t st) {
-    const int grid = dims.B * dims.C * dims.tilesX * dims.tilesY;
-    GVR_LAUNCH(st, "k_bwd_pixels",
-               (k_bwd_pixels<MODE, SHADED, TARGET, ALBPOS><<<grid, kTilePix, 0, st>>>(topo, dims, ws, io)));
-    return cudaGetLastError();
+// Calls v.run<MODE, SHADED, TARGET, ALBPOS>() for the pixel-kernel variant of
+// a call: MODE is the albedo class (vertex colour, nearest texture, bilinear
+// texture, or the constant white of foregroundMask), ALBPOS exists for
+// vertex colours only.
+template <int MODE, bool ALBPOS, class V>
+static cudaError_t visit_st(bool shaded, bool target, V &v) {
+    if (shaded) return target ? v.template run<MODE, true, true, ALBPOS>() : v.template run<MODE, true, false, ALBPOS>();
+    return target ? v.template run<MODE, false, true, ALBPOS>() : v.template run<MODE, false, false, ALBPOS>();
 }
 
-template <int MODE, bool ALBPOS>
-static cudaError_t launch_pixels_a(bool shaded, bool target, const Topology &topo, const FrameDims &dims,
-                                   const BwdScratch &ws, const BwdIO &io, cudaStream_t st) {
-    if (shaded) return target ? launch_pixels_t<MODE, true, true, ALBPOS>(topo, dims, ws, io, st)
-                              : launch_pixels_t<MODE, true, false, ALBPOS>(topo, dims, ws, io, st);
-    return target ? launch_pixels_t<MODE, false, true, ALBPOS>(topo, dims, ws, io, st)
-                  : launch_pixels_t<MODE, false, false, ALBPOS>(topo, dims, ws, io, st);
+template <class V>
+static cudaError_t visit_variant(int albedo, bool shaded, bool target, bool albpos, V &v) {
+    switch (albedo) {
+        case GVR_ALBEDO_VERTEX_COLOR:
+            return albpos ? visit_st<GVR_ALBEDO_VERTEX_COLOR, true>(shaded, target, v)
+                          : visit_st<GVR_ALBEDO_VERTEX_COLOR, false>(shaded, target, v);
+        case GVR_ALBEDO_TEXTURED: return visit_st<GVR_ALBEDO_TEXTURED, false>(shaded, target, v);
+        case GVR_ALBEDO_TEXTURED_BILINEAR: return visit_st<GVR_ALBEDO_TEXTURED_BILINEAR, false>(shaded, target, v);
+        default: return visit_st<GVR_ALBEDO_FOREGROUND_MASK, false>(false, target, v);
+    }
 }
 
-template <int MODE>
-static cudaError_t launch_pixels_m(bool shaded, bool target, bool albpos, const Topology &topo, const FrameDims &dims,
-                                   const BwdScratch &ws, const BwdIO &io, cudaStream_t st) {
-    if constexpr (MODE == GVR_ALBEDO_VERTEX_COLOR)
-        if (albpos) return launch_pixels_a<MODE, true>(shaded, target, topo, dims, ws, io, st);
-    return launch_pixels_a<MODE, false>(shaded, target, topo, dims, ws, io, st);
+// shaded: SH shading of a lit albedo (foregroundMask is forced shadeless)
+static bool backward_shaded(int albedo, int shading) {
+    return shading == GVR_SHADING_SHADED && albedo != GVR_ALBEDO_FOREGROUND_MASK;
 }
+
+int backward_variant(int albedo, int shading, bool target, bool albpos) {
+    if (albedo == GVR_ALBEDO_NORMAL || albedo == GVR_ALBEDO_LIGHTING || albedo == GVR_ALBEDO_UV) return -1;
+    const int cls = albedo == GVR_ALBEDO_VERTEX_COLOR ? 0 : albedo == GVR_ALBEDO_TEXTURED ? 1
+                  : albedo == GVR_ALBEDO_TEXTURED_BILINEAR ? 2 : 3;
+    const bool shaded = backward_shaded(albedo, shading);
+    const bool ap = albpos && albedo == GVR_ALBEDO_VERTEX_COLOR;
+    return ((cls * 2 + shaded) * 2 + target) * 2 + ap;
+}
+
+// The albedo mode, shading and options a variant number stands for.
+static void variant_parts(int variant, int &albedo, bool &shaded, bool &target, bool &albpos) {
+    static const int kCls[4] = {GVR_ALBEDO_VERTEX_COLOR, GVR_ALBEDO_TEXTURED, GVR_ALBEDO_TEXTURED_BILINEAR,
+                                GVR_ALBEDO_FOREGROUND_MASK};
+    albpos = variant & 1;
+    target = (variant >> 1) & 1;
+    shaded = (variant >> 2) & 1;
+    albedo = kCls[(variant >> 3) & 3];
+}
+
+struct CallPixels {
+    const Topology &topo;
+    const FrameDims &dims;
+    const BwdScratch &ws;
+    const BwdIO &io;
+    cudaStream_t st;
+    template <int MODE, bool SHADED, bool TARGET, bool ALBPOS>
+    cudaError_t run() {
+        const int BC = dims.B * dims.C;
+        for (int bc0 = 0; bc0 < BC; bc0 += 65535) {  // gridDim.z holds at most 65535 views
+            const dim3 grid(dims.tilesX, dims.tilesY, min(65535, BC - bc0));
+            GVR_LAUNCH(st, "k_bwd_pixels",
+                       (k_bwd_pixels<MODE, SHADED, TARGET, ALBPOS><<<grid, kTilePix, 0, st>>>(topo, dims, ws, io, bc0)));
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+};
+
+struct BatchedPixels {
+    const BwdBatchLaunch &L;
+    int g;
+    cudaStream_t st;
+    template <int MODE, bool SHADED, bool TARGET, bool ALBPOS>
+    cudaError_t run() {
+        GVR_LAUNCH(st, "k_bwd_pixels_batched",
+                   (k_bwd_pixels_batched<MODE, SHADED, TARGET, ALBPOS><<<L.groupBlocks[g], kTilePix, 0, st>>>(
+                       L.jobs, L.groupJobs[g], L.groupStart[g], L.groupCount[g])));
+        return cudaGetLastError();
+    }
+};
 
 cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const GvrBackwardArgs &a,
                             int imageFilter, cudaStream_t st) {
@@ -547,7 +678,7 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
         if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
         return cudaMemsetAsync(a.sh_coeff_grad, 0, (size_t)B * C * 27 * sizeof(float), st);
     }
-    const bool shaded = dims.shading == GVR_SHADING_SHADED && dims.albedo != GVR_ALBEDO_FOREGROUND_MASK;
+    const bool shaded = backward_shaded(dims.albedo, dims.shading);
     const bool target = a.target_grad != nullptr;
     if ((err = cudaMemsetAsync(ws.faceAcc, 0, (size_t)B * F * kFaceAccFloats * sizeof(float), st))) return err;
     if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
@@ -557,19 +688,8 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     BwdIO io{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image, a.vertex_normal,
              a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter, phong};
     const bool albpos = (a.flags & GVR_BACKWARD_ALBEDO_POSITION) != 0;
-    switch (dims.albedo) {
-        case GVR_ALBEDO_VERTEX_COLOR:
-            err = launch_pixels_m<GVR_ALBEDO_VERTEX_COLOR>(shaded, target, albpos, topo, dims, ws, io, st);
-            break;
-        case GVR_ALBEDO_TEXTURED:
-            err = launch_pixels_m<GVR_ALBEDO_TEXTURED>(shaded, target, false, topo, dims, ws, io, st);
-            break;
-        case GVR_ALBEDO_TEXTURED_BILINEAR:
-            err = launch_pixels_m<GVR_ALBEDO_TEXTURED_BILINEAR>(shaded, target, false, topo, dims, ws, io, st);
-            break;
-        default: err = launch_pixels_m<GVR_ALBEDO_FOREGROUND_MASK>(false, target, false, topo, dims, ws, io, st); break;
-    }
-    if (err) return err;
+    CallPixels call{topo, dims, ws, io, st};
+    if ((err = visit_variant(dims.albedo, shaded, target, albpos, call))) return err;
     GVR_LAUNCH(st, "k_gather_a",
                k_gather_a<<<blocks((size_t)B * N, 256), 256, 0, st>>>(
                    topo, B, reinterpret_cast<const float *>(ws.faceAcc), a.vertex_pos_grad, a.vertex_color_grad, ws.gN,
@@ -582,6 +702,41 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     }
     GVR_LAUNCH(st, "k_sh_finalize", k_sh_finalize<<<B * C * 27, 256, 0, st>>>(ws.shPartial, a.sh_coeff_grad, T, shaded));
     return cudaGetLastError();
+}
+
+// The batched backward of many jobs: one clearing launch, the camera and face
+// stages over every job, one pixel launch per variant present, both gathers
+// and the SH sums over every job.
+cudaError_t launch_backward_batched(const BwdBatchLaunch &L, cudaStream_t st) {
+    cudaError_t err;
+    if (L.zeroBlocks > 0) {
+        GVR_LAUNCH(st, "k_zero_regions", k_zero_regions<<<L.zeroBlocks, 256, 0, st>>>(L.zeros, L.zeroStart, L.nZero));
+        if ((err = cudaGetLastError())) return err;
+    }
+    if ((err = launch_bwd_geo_batched(L, st))) return err;
+    for (int g = 0; g < L.nGroups; ++g) {
+        int albedo;
+        bool shaded, target, albpos;
+        variant_parts(L.groupVariant[g], albedo, shaded, target, albpos);
+        BatchedPixels launch{L, g, st};
+        if ((err = visit_variant(albedo, shaded, target, albpos, launch))) return err;
+    }
+    if (L.blocks[kBStageVertices] > 0) {
+        GVR_LAUNCH(st, "k_gather_a_batched",
+                   k_gather_batched<0><<<L.blocks[kBStageVertices], 256, 0, st>>>(L.jobs, L.blockStart[kBStageVertices],
+                                                                                   L.nJobs));
+        if ((err = cudaGetLastError())) return err;
+        GVR_LAUNCH(st, "k_gather_b_batched",
+                   k_gather_batched<1><<<L.blocks[kBStageVertices], 256, 0, st>>>(L.jobs, L.blockStart[kBStageVertices],
+                                                                                   L.nJobs));
+        if ((err = cudaGetLastError())) return err;
+    }
+    if (L.blocks[kBStageSH] > 0) {
+        GVR_LAUNCH(st, "k_sh_finalize_batched",
+                   k_sh_finalize_batched<<<L.blocks[kBStageSH], 256, 0, st>>>(L.jobs, L.blockStart[kBStageSH], L.nJobs));
+        if ((err = cudaGetLastError())) return err;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace gvr

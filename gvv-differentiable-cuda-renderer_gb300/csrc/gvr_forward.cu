@@ -440,17 +440,6 @@ __global__ void k_bin_fill(const FwdJob J) {
 
 // ---------------------------------------------------------------------------- batched kernels
 
-// The job owning block `blk`: the last j with blockStart[j] <= blk.
-__device__ __forceinline__ int job_of_block(const int *__restrict__ blockStart, int nJobs, int blk) {
-    int lo = 0, hi = nJobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (blockStart[mid] <= blk) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 // Index spaces of the batched stages (BatchStage) and their per-job counts.
 __device__ __forceinline__ int stage_count(const FwdJob &J, int stage) {
     switch (stage) {
@@ -473,6 +462,22 @@ __global__ void __launch_bounds__(kBatchBlock) k_stage_batched(const FwdJob *__r
     else if (STAGE == kStageVertices) vertex_item(J, i);
     else if (STAGE == kStageBinCount) bin_count_item(J, i);
     else bin_fill_item(J, i);
+}
+
+// The backward's camera and face stages over every job of a batched plan
+// (zero-gradient jobs have no items).
+template <int STAGE>
+__global__ void __launch_bounds__(kBatchBlock) k_bwd_stage_batched(const BwdJob *__restrict__ jobs,
+                                                                   const int *__restrict__ blockStart, int nJobs) {
+    const int j = job_of_block(blockStart, nJobs, blockIdx.x);
+    const BwdJob &J = jobs[j];
+    const int i = (blockIdx.x - blockStart[j]) * kBatchBlock + threadIdx.x;
+    if (J.zeroMode) return;
+    if (STAGE == kBStageViews) {
+        if (i < J.dims.B * J.dims.C) camera_item(J.extr, J.intr, J.ws.cams, i);
+    } else if (i < J.dims.B * J.topo.F) {
+        face_geo_item(J.io.verts, J.topo.faces, J.ws.geo, nullptr, J.topo.N, J.topo.F, i, J.ws.faceRec, J.topo.uvs);
+    }
 }
 
 __global__ void __launch_bounds__(1024) k_scan_tiles_batched(const FwdJob *__restrict__ jobs) {
@@ -562,6 +567,23 @@ cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st) {
                    L.jobs, L.blockStart[kStageBinCount], L.nJobs));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     return launch_raster_persistent(L.jobs, L.itemStart, L.nJobs, L.counter, L.rasterGrid, st);
+}
+
+// Cameras and face records of every job of a batched backward.
+cudaError_t launch_bwd_geo_batched(const BwdBatchLaunch &L, cudaStream_t st) {
+    if (L.blocks[kBStageViews] > 0) {
+        GVR_LAUNCH(st, "k_cameras_bwd_batched",
+                   k_bwd_stage_batched<kBStageViews><<<L.blocks[kBStageViews], kBatchBlock, 0, st>>>(
+                       L.jobs, L.blockStart[kBStageViews], L.nJobs));
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+    }
+    if (L.blocks[kBStageFaces] > 0) {
+        GVR_LAUNCH(st, "k_face_geo_bwd_batched",
+                   k_bwd_stage_batched<kBStageFaces><<<L.blocks[kBStageFaces], kBatchBlock, 0, st>>>(
+                       L.jobs, L.blockStart[kBStageFaces], L.nJobs));
+    }
+    return cudaGetLastError();
 }
 
 // Per-pixel rays for tests (same pixel_ray as the raster).

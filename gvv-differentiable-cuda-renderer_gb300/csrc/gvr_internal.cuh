@@ -285,6 +285,17 @@ __device__ __forceinline__ float dot2(const float (&x)[K], const float (&y)[K]) 
     return __fadd_rn(p, s);
 }
 
+// The job owning block `blk` of a batched launch: the last j with blockStart[j] <= blk.
+__device__ __forceinline__ int job_of_block(const int *__restrict__ blockStart, int nJobs, int blk) {
+    int lo = 0, hi = nJobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (blockStart[mid] <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------------------- launch params
 
 struct Topology {
@@ -381,6 +392,24 @@ struct BwdIO {
     float *tex_grad;           // [B,Ht,Wt,3]
     int imageFilter;
     int phong;                 // GVR_SHADING_PHONG: albedo scaled by the headlight term, no SH
+};
+
+// One backward job of a batched plan: one handle's topology and one call's
+// frame, scratch and buffers.  The batched kernels read an array of them
+// from device memory.
+struct BwdJob {
+    Topology topo;
+    FrameDims dims;        // 16 x 16 tiles
+    BwdScratch ws;
+    BwdIO io;
+    const float *extr;     // [B,C,12]
+    const float *intr;     // [B,C,9]
+    float *vpos_grad;      // [B,N,3]
+    float *vcol_grad;      // [B,N,3]
+    float *sh_grad;        // [B,C,27]
+    int zeroMode;          // normal / lighting / UV: the outputs are only cleared
+    int shaded;            // SH terms and the normal-adjacency gather
+    int useCol;            // vertex colours receive a gradient
 };
 
 }  // namespace gvr

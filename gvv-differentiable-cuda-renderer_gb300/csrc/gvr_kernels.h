@@ -22,6 +22,43 @@ struct BatchLaunch {
     size_t zeroBytes;
 };
 
+// Stages of the batched backward, each with its own index space per job.
+enum BwdBatchStage { kBStageViews = 0, kBStageFaces, kBStageVertices, kBStageSH, kNumBwdStages };
+
+// A device region cleared by the batched backward (a gradient output or a
+// per-face accumulator), in floats.
+struct ZeroRegion {
+    float *ptr;
+    long long count;
+};
+constexpr int kZeroPerBlock = 4096;  // floats one block of the zeroing kernel clears
+
+// Variant of the backward pixel kernel: albedo class x shaded x target
+// gradient x albedo-through-barycentrics (see backward_variant).
+constexpr int kNumBwdVariants = 32;
+
+// Device tables of one batched backward (all pointers device memory).
+struct BwdBatchLaunch {
+    const BwdJob *jobs;                     // [nJobs]
+    const int *blockStart[kNumBwdStages];   // [nJobs + 1] first block of each job per stage
+    int blocks[kNumBwdStages];
+    const ZeroRegion *zeros;                // [nZero]
+    const int *zeroStart;                   // [nZero + 1] first block of each region
+    int nZero, zeroBlocks;
+    // the pixel kernel, one launch per variant present: jobs of the variant
+    // and their first tile blocks
+    int nGroups;
+    int groupVariant[kNumBwdVariants];
+    const int *groupJobs[kNumBwdVariants];  // [groupCount[g]] job indices
+    const int *groupStart[kNumBwdVariants]; // [groupCount[g] + 1]
+    int groupCount[kNumBwdVariants];
+    int groupBlocks[kNumBwdVariants];
+    int nJobs;
+};
+
+// The pixel-kernel variant of a backward call, or -1 for the zero-gradient modes.
+int backward_variant(int albedo, int shading, bool target, bool albpos);
+
 cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, int count, cudaStream_t st);
 cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *geo, float4 *fnormal, int B,
                             cudaStream_t st, float4 *bwdRec = nullptr);
@@ -32,6 +69,8 @@ cudaError_t launch_normal_map(const Topology &topo, const FrameDims &dims, int *
                               float *normal_map, int32_t *face, float *bary, float *render, cudaStream_t st);
 cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const GvrBackwardArgs &a,
                             int imageFilter, cudaStream_t st);
+cudaError_t launch_backward_batched(const BwdBatchLaunch &L, cudaStream_t st);
+cudaError_t launch_bwd_geo_batched(const BwdBatchLaunch &L, cudaStream_t st);
 cudaError_t launch_raster(const FwdJob &J, cudaStream_t st);
 cudaError_t launch_raster_persistent(const FwdJob *jobs, const int *itemStart, int nJobs, int *counter, int grid,
                                      cudaStream_t st);

@@ -155,10 +155,10 @@ __device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f
     return depth_key(depth_quantised(abc, z.x, z.y, z.z), f);
 }
 
-// One tile of one view: item = bc * tiles + tile of job J (256 threads, one
+// Tile (tx, ty) of view bc (= batch * C + camera) of job J (256 threads, one
 // pixel each).  Shared by the per-call grid kernel and the persistent
 // batched kernel, so both produce the same bits.
-__device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
+__device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const int tx, const int ty) {
     const Topology &topo = J.topo;
     const FrameDims &dims = J.dims;
     const FwdScratch &ws = J.ws;
@@ -167,14 +167,14 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     __shared__ float sBucketLo[kChunk];
     __shared__ int sHist[kBuckets + 1];
     const int T = dims.tilesX * dims.tilesY;
-    const int tile = item % T, bc = item / T, b = bc / dims.C;
+    const int tile = ty * dims.tilesX + tx, b = bc / dims.C;
     const int tileW = dims.tileW, tileH = dims.tileH;
-    const int tileX0 = (tile % dims.tilesX) * tileW, tileY0 = (tile / dims.tilesX) * tileH;
+    const int tileX0 = tx * tileW, tileY0 = ty * tileH;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // Each warp owns an 8x4 block of the tile (tileW / 8 blocks across):
-    // fewer faces overlap it than a full-width strip of 32 pixels.
-    const int wAcross = tileW >> 3;
-    const int colLo = tileX0 + ((warp % wAcross) << 3), rowLo = tileY0 + ((warp / wAcross) << 2);
+    // Each warp owns an 8x4 block of the tile (tileW / 8 = 2^wShift blocks
+    // across): fewer faces overlap it than a full-width strip of 32 pixels.
+    const int wShift = dims.tileShift - 3;
+    const int colLo = tileX0 + ((warp & ((1 << wShift) - 1)) << 3), rowLo = tileY0 + ((warp >> wShift) << 2);
     const int colHi = colLo + 7, rowHi = rowLo + 3;
     const int u = colLo + (lane & 7), v = rowLo + (lane >> 3);
     const float px = u + 0.5f, py = v + 0.5f;
@@ -206,7 +206,10 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
     // pass: every kept entry with such a bound lies in it.
     const unsigned zr0 = ws.zRange[2 * bc], zr1 = ws.zRange[2 * bc + 1];
     const float lo = zr1 ? __uint_as_float(~zr0) : kInf, hi = zr1 ? __uint_as_float(zr1) : 0.0f;
-    const float scale = hi > lo ? (float)kBuckets / (hi - lo) : 0.0f;
+    // bucket scale and the bucket width pulled down by 0.1% (below): any
+    // rounding here is far inside the 0.25% slack of the bounds themselves
+    const float scale = hi > lo ? __fdividef((float)kBuckets, hi - lo) : 0.0f;
+    const float edge = scale > 0.0f ? __fdividef(0.999f, scale) : 0.0f;
     for (int k = tid; k <= kBuckets; k += kTilePix) sHist[k] = 0;
     // the view's camera and SH coefficients, read by every pixel of the
     // resolve and shading: staged once per tile
@@ -269,7 +272,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
             sE[pos] = E;
             // the bucket's lower edge, pulled down by 0.1% of its offset so rounding
             // in the bucket index can never leave a member below it
-            sBucketLo[pos] = q == 0 ? -kInf : q == 1 ? lo : lo + (float)(q - 1) * (0.999f / scale);
+            sBucketLo[pos] = q == 0 ? -kInf : q == 1 ? lo : lo + (float)(q - 1) * edge;
         }
         __syncthreads();
         for (int k = tid; k <= kBuckets; k += kTilePix) sHist[k] = 0;  // free until the next chunk's first barrier
@@ -495,8 +498,11 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int item) {
 
 }  // namespace
 
-// One block per tile of one call.
-__global__ void __launch_bounds__(kTilePix, 4) k_raster(const FwdJob J) { raster_tile(J, blockIdx.x); }
+// One block per tile of one call: grid (tilesX, tilesY, views), views
+// bcBase .. bcBase + gridDim.z - 1.
+__global__ void __launch_bounds__(kTilePix, 5) k_raster(const FwdJob J, int bcBase) {
+    raster_tile(J, bcBase + blockIdx.z, blockIdx.x, blockIdx.y);
+}
 
 // Persistent: a grid sized to the resident capacity pulls (job, view, tile)
 // items from one counter until all jobs' tiles are done.  itemStart[j] is the
@@ -504,7 +510,7 @@ __global__ void __launch_bounds__(kTilePix, 4) k_raster(const FwdJob J) { raster
 __global__ void __launch_bounds__(kTilePix, 3) k_raster_persistent(const FwdJob *__restrict__ jobs,
                                                                 const int *__restrict__ itemStart, int nJobs,
                                                                 int *__restrict__ counter) {
-    __shared__ int sItem, sJob;
+    __shared__ int sItem, sJob, sBC, sTX, sTY;
     __shared__ FwdJob sJ;
     const int total = itemStart[nJobs];
     for (;;) {
@@ -519,6 +525,12 @@ __global__ void __launch_bounds__(kTilePix, 3) k_raster_persistent(const FwdJob 
                     else hi = mid - 1;
                 }
                 j = lo;
+                // (view, tile) of the item, decomposed once for the block
+                const FrameDims &d = jobs[j].dims;
+                const int local = item - itemStart[j], T = d.tilesX * d.tilesY, tile = local % T;
+                sBC = local / T;
+                sTX = tile % d.tilesX;
+                sTY = tile / d.tilesX;
             }
             sItem = item;
             sJob = j;
@@ -531,15 +543,20 @@ __global__ void __launch_bounds__(kTilePix, 3) k_raster_persistent(const FwdJob 
         for (int w = threadIdx.x; w < words; w += blockDim.x)
             reinterpret_cast<int *>(&sJ)[w] = reinterpret_cast<const int *>(jobs + j)[w];
         __syncthreads();
-        raster_tile(sJ, item - itemStart[j]);
+        raster_tile(sJ, sBC, sTX, sTY);
         __syncthreads();  // shared memory and sItem are reused by the next item
     }
 }
 
 cudaError_t launch_raster(const FwdJob &J, cudaStream_t st) {
-    const int grid = J.dims.B * J.dims.C * J.dims.tilesX * J.dims.tilesY;
-    GVR_LAUNCH(st, "k_raster", k_raster<<<grid, kTilePix, 0, st>>>(J));
-    return cudaGetLastError();
+    const int BC = J.dims.B * J.dims.C;
+    for (int bc0 = 0; bc0 < BC; bc0 += 65535) {  // gridDim.z holds at most 65535 views
+        const dim3 grid(J.dims.tilesX, J.dims.tilesY, min(65535, BC - bc0));
+        GVR_LAUNCH(st, "k_raster", k_raster<<<grid, kTilePix, 0, st>>>(J, bc0));
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_raster_persistent(const FwdJob *jobs, const int *itemStart, int nJobs, int *counter, int grid,

@@ -65,7 +65,7 @@ EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forw
            "gvr_backward_workspace_size", "gvr_last_error", "gvr_abi_version", "gvr_debug_rays",
            "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc",
            "gvr_plan_create", "gvr_plan_forward", "gvr_plan_forward_graph", "gvr_plan_tile_config",
-           "gvr_plan_destroy", "gvr_image_gradient", "gvr_image_gaussian3x3",
+           "gvr_plan_bind_backward", "gvr_plan_backward", "gvr_plan_backward_graph", "gvr_plan_destroy", "gvr_image_gradient", "gvr_image_gaussian3x3",
            # include/gvr_nn.h
            "gvr_gemm_bf16", "gvr_tc_error", "gvr_tc_wait_probe", "gvr_im2col_3x3s2", "gvr_col2im_3x3s2", "gvr_nn_last_error")
 
@@ -119,6 +119,12 @@ def load(build_if_missing: bool = True):
     I32P = ctypes.POINTER(I32)
     L.gvr_plan_tile_config.argtypes = [P, I32, I32P, I32P, I32P]
     L.gvr_plan_tile_config.restype = ctypes.c_int
+    L.gvr_plan_bind_backward.argtypes = [P, ctypes.POINTER(GvrBackwardArgs), I32]
+    L.gvr_plan_bind_backward.restype = ctypes.c_int
+    L.gvr_plan_backward.argtypes = [P, P]
+    L.gvr_plan_backward.restype = ctypes.c_int
+    L.gvr_plan_backward_graph.argtypes = [P, P]
+    L.gvr_plan_backward_graph.restype = ctypes.c_int
     L.gvr_plan_destroy.argtypes = [P]
     L.gvr_plan_destroy.restype = None
     L.gvr_image_gradient.argtypes = [P, P, P, I32, I32, I32, P]

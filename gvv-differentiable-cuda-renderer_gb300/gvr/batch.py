@@ -1,4 +1,4 @@
-"""Batched forward of many meshes through one plan (gvr_plan_* in include/gvr.h).
+"""Batched forward and backward of many meshes through one plan (gvr_plan_* in include/gvr.h).
 
 The reference renders one mesh per op call and loops over the batch on the
 host (cpp/src/TensorflowOperators/CudaRenderer/CudaRenderer.cpp:309).  A
@@ -6,6 +6,9 @@ BatchPlan binds many jobs -- each a RendererHandle (mesh, views, resolution,
 modes) with its own inputs -- once, and renders them all with one launch per
 pipeline stage and one persistent raster kernel, optionally replayed as a
 captured CUDA graph.  Each job's outputs equal render_forward's bit for bit.
+The backward (cpp/src/TensorflowOperators/CudaRenderer/CudaRendererGrad.cpp:259
+loops the same way) is batched likewise: bind one backward call per job,
+then one launch per stage and per pixel-kernel variant.
 """
 from __future__ import annotations
 
@@ -97,6 +100,68 @@ class BatchPlan:
             args.workspace_bytes = self._ws.numel()
             _lib.check(self._L.gvr_forward(h.ptr, ctypes.byref(args), s))
         return self.outputs
+
+    def bind_backward(self, grad_render, grad_target=None, target_image=None, flags=0):
+        """Binds one backward call per job: grad_render[j] [B,C,H,W,3] (the
+        upstream gradient of job j's render), optionally grad_target[j] and
+        target_image[j] (the model-to-data term; None entries leave it out)
+        and the GVR_BACKWARD_* flags.  Uses the plan's inputs and the
+        forward's outputs (face ids, vertex normals).  Gradients land in
+        self.grads[j] (vertex_pos, vertex_color, texture, sh_coeff); update
+        self.grad_inputs[j] in place between calls."""
+        J = len(self.handles)
+        gt = grad_target if grad_target is not None else [None] * J
+        ti = target_image if target_image is not None else [None] * J
+        arr = (_lib.GvrBackwardArgs * J)()
+        self.grad_inputs, self.grads = [], []
+        for j, h in enumerate(self.handles):
+            inp, out = self.inputs[j], self.outputs[j]
+            dev = h.device
+            B = int(inp["vertex_pos"].shape[0])
+            tex = inp["texture"]
+            Ht, Wt = (int(tex.shape[1]), int(tex.shape[2])) if tex is not None else (1, 1)
+            g = dict(grad_render=_as_f32(grad_render[j], dev, (B, h.C, h.H, h.W, 3)),
+                     grad_target=_as_f32(gt[j], dev, (B, h.C, h.H, h.W, 3)) if gt[j] is not None else None,
+                     target_image=_as_f32(ti[j], dev, (B, h.C, h.H, h.W, 3)) if ti[j] is not None else None)
+            o = dict(vertex_pos=torch.empty((B, h.N, 3), device=dev), vertex_color=torch.empty((B, h.N, 3), device=dev),
+                     texture=torch.empty((B, Ht, Wt, 3), device=dev), sh_coeff=torch.empty((B, h.C, 27), device=dev))
+            arr[j] = _lib.GvrBackwardArgs(B, Ht, Wt, _ptr(g["grad_render"]), _ptr(inp["vertex_pos"]),
+                                          _ptr(inp["vertex_color"]), _ptr(tex), _ptr(inp["sh_coeff"]),
+                                          _ptr(g["target_image"]), _ptr(out["vertex_normal"]), _ptr(out["barycentric"]),
+                                          _ptr(out["face"]), _ptr(g["grad_target"]), _ptr(inp["extrinsics"]),
+                                          _ptr(inp["intrinsics"]), _ptr(o["vertex_pos"]), _ptr(o["vertex_color"]),
+                                          _ptr(o["texture"]), _ptr(o["sh_coeff"]), None, 0, int(flags))
+            self.grad_inputs.append(g)
+            self.grads.append(o)
+        self._bwd_args = arr
+        with torch.cuda.device(self.device):
+            _lib.check(self._L.gvr_plan_bind_backward(self._plan, arr, J))
+
+    def backward(self, stream=None, graph=False):
+        """Gradients of every bound job on `stream`; graph=True captures the
+        batched backward into a CUDA graph on the first call and replays it
+        afterwards (needs a non-default stream)."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        s = ctypes.c_void_p(st.cuda_stream)
+        fn = self._L.gvr_plan_backward_graph if graph else self._L.gvr_plan_backward
+        _lib.check(fn(self._plan, s))
+        return self.grads
+
+    def backward_per_call(self, stream=None):
+        """The bound backward calls through gvr_backward one by one (the
+        reference's per-element loop), into the same gradient buffers."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        s = ctypes.c_void_p(st.cuda_stream)
+        if not hasattr(self, "_bws"):
+            need = max(int(self._L.gvr_backward_workspace_size(h.ptr, self._bwd_args[j].batch, 0, 0))
+                       for j, h in enumerate(self.handles))
+            self._bws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.device)
+        for j, h in enumerate(self.handles):
+            args = _lib.GvrBackwardArgs.from_buffer_copy(self._bwd_args[j])
+            args.workspace = ctypes.c_void_p(self._bws.data_ptr())
+            args.workspace_bytes = self._bws.numel()
+            _lib.check(self._L.gvr_backward(h.ptr, ctypes.byref(args), s))
+        return self.grads
 
     def tile_config(self, j):
         w, h, b = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -256,6 +256,27 @@ int gvr_plan_forward(GvrPlan *plan, void *stream);
 int gvr_plan_forward_graph(GvrPlan *plan, void *stream);
 /* The bin/tile configuration chosen for job `job`. */
 int gvr_plan_tile_config(const GvrPlan *plan, int32_t job, int32_t *tile_w, int32_t *tile_h, int32_t *big_tiles);
+
+/* Batched backward of the same jobs (no reference counterpart: the reference
+ * runs its grad op once per batch element in a host loop,
+ * cpp/src/TensorflowOperators/CudaRenderer/CudaRendererGrad.cpp:259-285).
+ * gvr_plan_bind_backward binds one backward call per job of the plan, in
+ * the plan's job order (`count` = the plan's job count; the arguments mean
+ * what they mean for gvr_backward, workspace fields ignored) and allocates
+ * every job's scratch; binding again replaces the earlier binding.
+ * gvr_plan_backward then computes every job's gradients with one clearing
+ * launch, one launch per stage over all jobs (cameras, face records, the
+ * two vertex gathers, the SH sums) and one pixel-kernel launch per kernel
+ * variant present among the jobs (albedo class x shaded x target gradient),
+ * allocating nothing and never synchronising the host;
+ * gvr_plan_backward_graph captures that sequence once into a CUDA graph and
+ * replays it.  Each job's gradients equal gvr_backward's on the same
+ * buffers up to the order of the FP32 atomic sums (SH gradients bit for
+ * bit).  The bound buffers must stay valid for the life of the binding. */
+int gvr_plan_bind_backward(GvrPlan *plan, const GvrBackwardArgs *args, int32_t count);
+int gvr_plan_backward(GvrPlan *plan, void *stream);
+/* `stream` must be a created stream (graph capture cannot use the legacy default stream). */
+int gvr_plan_backward_graph(GvrPlan *plan, void *stream);
 void gvr_plan_destroy(GvrPlan *plan);
 
 /* Per-kernel timing, no reference counterpart.  While enabled, every kernel

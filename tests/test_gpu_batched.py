@@ -180,3 +180,150 @@ def test_full_uneven_workload_against_single_calls_and_oracle():
         assert _same(out["vertex_normal"].cpu().numpy()[0, c], ref["vertex_normal"][0]), (j, c)
         assert rel_max(out["render"].cpu().numpy()[0, c], ref["render"][0]) <= 1e-5, (j, c)
     plan.close()
+
+
+# ---------------------------------------------------------------------------- batched backward
+
+GRAD_KEYS = ("vertex_pos", "vertex_color", "texture", "sh_coeff")
+
+
+def _grads_per_call(plan, j):
+    """render_backward of job j on the plan's buffers (the reference's per-element call)."""
+    import torch
+    from gvr import renderer
+    inp, out, g = plan.inputs[j], plan.outputs[j], plan.grad_inputs[j]
+    h = plan.handles[j]
+    tex = inp["texture"] if inp["texture"] is not None else torch.zeros((inp["vertex_pos"].shape[0], 1, 1, 3),
+                                                                      device=h.device)
+    vc = inp["vertex_color"] if inp["vertex_color"] is not None else torch.zeros_like(inp["vertex_pos"])
+    r = renderer.render_backward(h, g["grad_render"], inp["vertex_pos"], vc, tex, inp["sh_coeff"], g["target_image"],
+                                 out["vertex_normal"], out["barycentric"], out["face"], g["grad_target"],
+                                 inp["extrinsics"], inp["intrinsics"])
+    torch.cuda.synchronize()
+    return dict(zip(GRAD_KEYS, (x.cpu().numpy() for x in r)))
+
+
+def _check_grads(plan, jobs, rng=None, oracle_sample=0):
+    """Every job: the batched gradients equal the per-call backward up to the
+    order of FP32 atomic sums (||a - b|| <= 1e-6 ||b||; SH bit for bit);
+    `oracle_sample` jobs also against the FP64 oracle at the parity bar."""
+    import torch
+    from helpers import oracle_scene, rel_norm
+    torch.cuda.synchronize()
+    for j in range(len(jobs)):
+        ref = _grads_per_call(plan, j)
+        got = {k: plan.grads[j][k].cpu().numpy() for k in GRAD_KEYS}
+        assert _same(got["sh_coeff"], ref["sh_coeff"]), (j, "sh_coeff")
+        for k in GRAD_KEYS:
+            if np.all(ref[k] == 0):
+                assert np.all(got[k] == 0), (j, k)
+            else:
+                assert rel_norm(got[k], ref[k]) <= 1e-6, (j, k, rel_norm(got[k], ref[k]))
+    if oracle_sample and rng is not None:
+        for j in rng.choice(len(jobs), size=min(oracle_sample, len(jobs)), replace=False):
+            s = jobs[int(j)]["spec"]
+            out, g = plan.outputs[j], plan.grad_inputs[j]
+            rays = plan.handles[j].debug_rays(plan.inputs[j]["extrinsics"], plan.inputs[j]["intrinsics"]).cpu().numpy()
+            o = oracle_scene(s, 0, rays=rays[0])
+            gt = g["grad_target"].cpu().numpy()[0] if g["grad_target"] is not None else \
+                np.zeros(g["grad_render"].shape[1:], np.float32)
+            tgt = g["target_image"].cpu().numpy()[0] if g["target_image"] is not None else np.zeros_like(gt)
+            orc = o.backward(out["face"].cpu().numpy()[0], out["barycentric"].cpu().numpy()[0],
+                             out["vertex_normal"].cpu().numpy()[0], g["grad_render"].cpu().numpy()[0], tgt, gt)
+            for k in GRAD_KEYS:
+                mine, theirs = plan.grads[j][k].cpu().numpy()[0], orc[k + "_grad"]
+                if np.all(theirs == 0):
+                    assert np.all(mine == 0), (int(j), k)
+                else:
+                    assert rel_norm(mine, theirs) <= 1e-4, (int(j), k, rel_norm(mine, theirs))
+
+
+def _bind_random_backward(plan, specs, rng, target_every=3):
+    grads, targets, images = [], [], []
+    for j, s in enumerate(specs):
+        shape = (1, s["num_views"], s["height"], s["width"], 3)
+        grads.append(rng.normal(0, 1, shape).astype(np.float32))
+        with_t = j % target_every == 1
+        targets.append(rng.normal(0, 1, shape).astype(np.float32) if with_t else None)
+        images.append(rng.uniform(0, 1, shape).astype(np.float32) if with_t else None)
+    plan.bind_backward(grads, targets, images)
+
+
+def test_plan_backward_matches_single_calls_and_oracle():
+    """Mixed modes (every albedo x shading mode of the reference, with and
+    without the model-to-data term) through one batched backward."""
+    import torch
+    from gvr.batch import BatchPlan
+    dev = torch.device("cuda", 0)
+    specs = _jobs(seed=13, meshes=8)
+    jobs = _plan_jobs(specs, dev)
+    for j, s in zip(jobs, specs):
+        j["spec"] = s
+    plan = BatchPlan([{k: v for k, v in j.items() if k != "spec"} for j in jobs])
+    plan.forward()
+    rng = np.random.default_rng(13)
+    _bind_random_backward(plan, specs, rng)
+    plan.backward()
+    _check_grads(plan, jobs, rng, oracle_sample=4)
+    plan.close()
+
+
+def test_plan_backward_graph_replay_follows_new_gradients():
+    import torch
+    from gvr.batch import BatchPlan
+    dev = torch.device("cuda", 0)
+    specs = _jobs(seed=17, meshes=5)
+    jobs = _plan_jobs(specs, dev)
+    plan = BatchPlan(jobs)
+    stream = torch.cuda.Stream(dev)
+    rng = np.random.default_rng(17)
+    with torch.cuda.stream(stream):
+        plan.forward(stream=stream, graph=True)
+        _bind_random_backward(plan, specs, rng)
+        plan.backward(stream=stream, graph=True)
+    stream.synchronize()
+    _check_grads(plan, jobs)
+    for g in plan.grad_inputs:                       # new upstream gradients, same buffers
+        g["grad_render"].mul_(-0.5).add_(0.25)
+    with torch.cuda.stream(stream):
+        plan.backward(stream=stream, graph=True)
+    stream.synchronize()
+    _check_grads(plan, jobs)
+    plan.close()
+
+
+def test_plan_backward_refuses_a_wrong_job_count():
+    import ctypes
+    import torch
+    from gvr import _lib
+    from gvr.batch import BatchPlan
+    dev = torch.device("cuda", 0)
+    plan = BatchPlan(_plan_jobs(_jobs(seed=3, meshes=2), dev))
+    L = _lib.load()
+    assert L.gvr_plan_bind_backward(plan._plan, (_lib.GvrBackwardArgs * 1)(), 1) == -1
+    assert L.gvr_plan_backward(plan._plan, None) == -1          # nothing bound
+    plan.close()
+
+
+def test_full_uneven_workload_backward():
+    """The batched bench's whole uneven workload, forward and backward through
+    the plan's graphs: every job's gradients equal the per-call backward,
+    four sampled jobs equal the FP64 oracle."""
+    import torch
+    from gvr import scenes
+    from gvr.batch import BatchPlan
+    dev = torch.device("cuda", 0)
+    specs = scenes.uneven_batch(seed=0, num_meshes=64)
+    jobs = _plan_jobs(specs, dev)
+    for j, s in zip(jobs, specs):
+        j["spec"] = s
+    plan = BatchPlan([{k: v for k, v in j.items() if k != "spec"} for j in jobs], autotune=True)
+    stream = torch.cuda.Stream(dev)
+    rng = np.random.default_rng(29)
+    with torch.cuda.stream(stream):
+        plan.forward(stream=stream, graph=True)
+        _bind_random_backward(plan, specs, rng, target_every=7)
+        plan.backward(stream=stream, graph=True)
+    stream.synchronize()
+    _check_grads(plan, jobs, rng, oracle_sample=4)
+    plan.close()
