@@ -53,11 +53,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     ap.add_argument("--views", type=int, default=8, help="views of the workload (profiling runs use fewer)")
-    ap.add_argument("--workload", choices=["multiview", "batched", "fit", "learned"], default="multiview",
+    ap.add_argument("--workload", choices=["multiview", "batched", "fit", "learned", "gemm"], default="multiview",
                     help="multiview: the fwd+bwd step above (default); batched: 64 uneven meshes through one "
                          "plan (forward + backward), against the same jobs as one call each; fit: plain "
                          "analysis-by-synthesis fits of the morphable model; learned: train the proposal "
-                         "network, then fit from its proposals against the plain fit")
+                         "network, then fit from its proposals against the plain fit; gemm: the proposal "
+                         "network's GEMM shapes on the tcgen05 kernel and on torch.matmul")
     ap.add_argument("--meshes", type=int, default=64, help="meshes of the batched workload")
     ap.add_argument("--fits", type=int, default=1000, help="held-out seeds of the fit / learned workloads")
     ap.add_argument("--train-renders", type=int, default=1_000_000, help="renders the proposal network trains on")
@@ -663,6 +664,83 @@ def run_fit_bench(args):
         print(json.dumps(line), flush=True)
 
 
+def run_gemm_bench(args):
+    """The proposal network's matrix products at its real shapes (training
+    batch 256, 256x256 input): the five im2col convolutions (forward, input
+    gradient, weight gradient), the two MLP layers, and the first MLP
+    layer's gradients.  Each on the tcgen05 GEMM (gvr_gemm_bf16 through
+    gvr.tc.gemm, which splits K for the weight gradients as the network's
+    calls do; BF16 operands, FP32 accumulate, operands already K-padded) and
+    on torch.matmul (cuBLAS) with the same BF16 operands and output type;
+    CUDA events, median of `--steps` launches after warm-up.  Reports
+    TFLOP/s (2 M N K / t) and the GB/s of the minimal traffic (both operands
+    read once, the output written once) against the measured peaks."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from gvr import native_build, tc
+    native_build.build()
+    B = 256
+    shapes = []  # (name, M, N, K, output type)
+    chans = (3, 32, 64, 128, 256, 256)
+    hw = 256
+    for i, (ci, co) in enumerate(zip(chans[:-1], chans[1:])):
+        hw //= 2
+        K = (9 * ci + 63) // 64 * 64
+        M = B * hw * hw
+        shapes.append((f"conv{i + 1} fwd", M, co, K, torch.bfloat16))
+        shapes.append((f"conv{i + 1} dgrad", M, K, co if co % 64 == 0 else 64, torch.float32))
+        shapes.append((f"conv{i + 1} wgrad", co, K, M, torch.float32))
+    shapes += [("fc1 fwd", B, 1024, 16384, torch.float32), ("fc1 dgrad", B, 16384, 1024, torch.float32),
+               ("fc1 wgrad", 1024, 16384, B, torch.float32), ("fc2 fwd", B, 193, 1024, torch.float32)]
+    peaks = {}
+    pk = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    rows = []
+    gen = torch.Generator(device=dev).manual_seed(0)
+
+    def timed(fn, reps):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    for name, M, N, K, odt in shapes:
+        A = (torch.randn((M, K), generator=gen, device=dev) * 0.1).to(torch.bfloat16)
+        Bm = (torch.randn((N, K), generator=gen, device=dev) * 0.1).to(torch.bfloat16)
+        ours = timed(lambda: tc.gemm(A, Bm, out_dtype=odt), args.steps)
+        ref = timed(lambda: torch.matmul(A, Bm.t()).to(odt), args.steps)
+        exact = torch.matmul(A.float(), Bm.float().t())
+        err = float((tc.gemm(A, Bm, out_dtype=torch.float32) - exact).abs().max() / exact.abs().max())
+        flops = 2.0 * M * N * K
+        byts = 2.0 * (M * K + N * K) + M * N * (2 if odt == torch.bfloat16 else 4)
+        rows.append({"gemm": name, "M": M, "N": N, "K": K, "ours_ms": ours, "ours_tflops": flops / ours / 1e9,
+                     "ours_gbs": byts / ours / 1e6, "torch_ms": ref, "torch_tflops": flops / ref / 1e9,
+                     "torch_gbs": byts / ref / 1e6, "rel_err_vs_fp32": err})
+        del A, Bm, exact
+    tot_ours = sum(r["ours_ms"] for r in rows)
+    tot_ref = sum(r["torch_ms"] for r in rows)
+    line = {"metric": "proposal-network GEMM shape set, total ms (tcgen05 GEMM; cuBLAS beside it)",
+            "value": tot_ours, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+            "higher_is_better": False, "scaling": "none", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+            "data": "synthetic N(0, 0.01) operands",
+            "config": {"workload": "proposal network GEMM shapes, batch 256, 256^2 input", "shapes": len(rows)},
+            "torch_matmul_ms": tot_ref, "ratio_torch_over_ours": tot_ref / tot_ours,
+            "peaks": {"bf16_tflops": peaks.get("bf16_tflops"), "hbm_gbs": peaks.get("hbm_gbs")}, "shapes": rows}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -671,6 +749,8 @@ def main():
         run_batched(args)
     elif args.workload in ("fit", "learned"):
         run_fit_bench(args)
+    elif args.workload == "gemm":
+        run_gemm_bench(args)
     else:
         run_gvr(args)
     if int(os.environ.get("WORLD_SIZE", "1")) > 1:

@@ -95,6 +95,7 @@ void fwd_carve_main(const GvrHandle *h, int B, int Ht, int Wt, const TileCfg &tc
         return;
     }
     L.s.vface = c.take<gvr::ViewFace>(BC * h->F);
+    L.s.shadeRec = c.take<float4>((size_t)B * h->F * gvr::kShadeRows);
     L.s.tileStart = c.take<int>(BC * T + 1);
     L.s.bins = c.take<int>((size_t)tc.big * BC * h->F);
     L.s.bigList = c.take<int>(BC * h->F);

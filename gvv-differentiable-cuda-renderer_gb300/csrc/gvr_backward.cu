@@ -242,7 +242,9 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                     wt[2] += ga[ch] * (c9[2] + c9[5] * n.y + 6.0f * c9[6] * n.z + c9[7] * n.x);
                 }
                 // . d(n)/d(un) = (|un|^2 I - un un^T) / |un|^3  (getJNoNu, :398-415)
-                const float len2 = len * len, inv3 = 1.0f / (len2 * len);
+                // the divisions of the continuous chain-rule terms use the hardware
+                // reciprocal (2 ulp): the gradients' bar is 1e-4 relative
+                const float len2 = len * len, inv3 = __fdividef(1.0f, len2 * len);
                 const float wdot = wt[0] * un.x + wt[1] * un.y + wt[2] * un.z;
                 wv[0] = (wt[0] * len2 - un.x * wdot) * inv3;
                 wv[1] = (wt[1] * len2 - un.y * wdot) * inv3;
@@ -288,13 +290,13 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                     const float wy = __fmaf_rn(t, d.y, -Dh[1]) - Dl[1];
                     const float wz = __fmaf_rn(t, d.z, -Dh[2]) - Dl[2];
                     // barycentrics of the hit point: b1 = (w x e2).N / N.N, b2 = (e1 x w).N / N.N
-                    const float inn = 1.0f / nn;
+                    const float inn = __fdividef(1.0f, nn);
                     const float hb1 = ((wy * e2.z - wz * e2.y) * Nf[0] + (wz * e2.x - wx * e2.z) * Nf[1] +
                                        (wx * e2.y - wy * e2.x) * Nf[2]) * inn;
                     const float hb2 = ((e1.y * wz - e1.z * wy) * Nf[0] + (e1.z * wx - e1.x * wz) * Nf[1] +
                                        (e1.x * wy - e1.y * wx) * Nf[2]) * inn;
                     const float hb[3] = {1.0f - hb1 - hb2, hb1, hb2};
-                    const float inv = 1.0f / nd;
+                    const float inv = __fdividef(1.0f, nd);
                     const float3 g1 = make_float3((e2.y * d.z - e2.z * d.y) * inv, (e2.z * d.x - e2.x * d.z) * inv,
                                                   (e2.x * d.y - e2.y * d.x) * inv);
                     const float3 g2 = make_float3((d.y * e1.z - d.z * e1.y) * inv, (d.z * e1.x - d.x * e1.z) * inv,
@@ -327,8 +329,8 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                             gv += gi * Gv;
                             norm += fabsf(Gu);
                         }
-                    gu /= norm;
-                    gv /= norm;
+                    gu = __fdividef(gu, norm);
+                    gv = __fdividef(gv, norm);
                     const float4 fr2 = FR[2], fr3 = FR[3], fr4 = FR[4];  // vertex positions
                     const float P0[3] = {fr2.y, fr2.z, fr2.w}, P1[3] = {fr3.x, fr3.y, fr3.z}, P2[3] = {fr3.w, fr4.x, fr4.y};
                     float X[3];
@@ -339,7 +341,7 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                     const float Py = KE[4] * X[0] + KE[5] * X[1] + KE[6] * X[2] + KE[7];
                     const float Pz = KE[8] * X[0] + KE[9] * X[1] + KE[10] * X[2] + KE[11];
                     if (fabsf(Pz) > 0.0001f) {
-                        const float iz = 1.0f / Pz, ax = Px * iz, ay = Py * iz;
+                        const float iz = __fdividef(1.0f, Pz), ax = Px * iz, ay = Py * iz;
 #pragma unroll
                         for (int a = 0; a < 3; ++a)
                             Pv[a] += (gu * (KE[a] - ax * KE[8 + a]) + gv * (KE[4 + a] - ay * KE[8 + a])) * iz;

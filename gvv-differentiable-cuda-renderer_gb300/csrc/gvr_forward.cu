@@ -261,6 +261,17 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
         const bool clear = fnLen * 1e-6f * cosv >= 4e-7f;
         flags = kScreenValid | ((cosv >= 0.02f && clear && mIn < 0.2f) ? kCertain : 0);
     }
+    if (bc - b * dims.C == 0) {  // view 0 writes the face's shading record (vertex normals of view 0)
+        const float *VN = J.vnormal_out + (size_t)bc * N * 3;
+        const float *t = topo.uvs + 6 * (size_t)f;
+        const V3 n0 = ld3(VN + 3 * i0), n1 = ld3(VN + 3 * i1), n2 = ld3(VN + 3 * i2);
+        float4 *R = ws.shadeRec + ((size_t)b * F + f) * kShadeRows;
+        R[0] = make_float4(n0.x, n0.y, n0.z, n1.x);
+        R[1] = make_float4(n1.y, n1.z, n2.x, n2.y);
+        R[2] = make_float4(n2.z, t[0], t[1], t[2]);
+        R[3] = make_float4(t[3], t[4], t[5], 0.0f);
+        R[4] = make_float4(__int_as_float(i0), __int_as_float(i1), __int_as_float(i2), 0.0f);
+    }
     ViewFace vf;
     vf.hdr = make_int4(box.x | (box.z << 16), box.y | (box.w << 16), flags, __float_as_int(dRel));
     vf.z = make_float4(p0.z, p1.z, p2.z, mIn);

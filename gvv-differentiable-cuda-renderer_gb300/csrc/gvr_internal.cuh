@@ -318,10 +318,19 @@ struct FrameDims {
 };
 
 // Forward scratch carved out of one workspace.
+// Per (batch, face) record of what the forward's shading reads about a
+// face, five 16-byte rows instead of 18 dependent scalar gathers:
+//   r0 = N0.xyz, N1.x;  r1 = N1.yz, N2.xy;  r2 = N2.z, u0, v0, u1;
+//   r3 = v1, u2, v2, 0;  r4 = i0, i1, i2 (int bits), 0
+// (N: the un-normalised vertex normals of view 0, bit-identical to the
+// vertex_normal output of every view; u, v: texture coordinates as stored).
+constexpr int kShadeRows = 5;
+
 struct FwdScratch {
     Camera *cams;        // [B*C]
     FaceGeo *geo;        // [B*F]
     float4 *fnormal;     // [B*F] un-normalised face normals
+    float4 *shadeRec;    // [B*F*kShadeRows], written by the binning pass
     ViewFace *vface;     // [B*C*F]
     int *tileCount;      // [B*C*T]
     int *tileStart;      // [B*C*T + 1]

@@ -418,27 +418,30 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
         return;
     }
     const int f = (int)(unsigned)(best & 0xffffffffull);
-    const int i0 = topo.faces[3 * f], i1 = topo.faces[3 * f + 1], i2 = topo.faces[3 * f + 2];
     io.face[p] = f;
     reinterpret_cast<float2 *>(io.bary)[p] = make_float2(abc.x, abc.y);
 
-    // shading (CUDABasedRasterization.cu:307-403)
+    // shading (CUDABasedRasterization.cu:307-403) from the face's shading record
+    const float4 *SR = ws.shadeRec + ((size_t)b * F + f) * kShadeRows;
+    const float4 r0 = SR[0], r1 = SR[1];
     const V3 d = x.d;
-    const float *VN = io.vnormal + (size_t)bc * topo.N * 3;
-    V3 un = pixel_normal_un(ld3(VN + 3 * i0), ld3(VN + 3 * i1), ld3(VN + 3 * i2), abc);
+    V3 un = pixel_normal_un(v3(r0.x, r0.y, r0.z), v3(r0.w, r1.x, r1.y), v3(r1.z, r1.w, SR[2].x), abc);
     float len = __fsqrt_rn(xdot(un, un));
     V3 n = v3(xd(un.x, len), xd(un.y, len), xd(un.z, len));
     if (xdot(n, d) > 0.0f) n = v3(-n.x, -n.y, -n.z);
     float3 col;
     switch (dims.albedo) {
         case GVR_ALBEDO_TEXTURED: {
-            float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+            const float4 r2 = SR[2], r3 = SR[3];
+            const float2 tc = texel_coord6(r2.y, r2.z, r2.w, r3.x, r3.y, r3.z, abc, dims.Wt, dims.Ht);
             int LU = __float2int_rz(xs(tc.x, 0.5f)), LV = __float2int_rz(xs(tc.y, 0.5f));
             const float *t = io.texture + (((size_t)b * dims.Ht + LV) * dims.Wt + LU) * 3;
             col = make_float3(t[0], t[1], t[2]);
             break;
         }
         case GVR_ALBEDO_VERTEX_COLOR: {
+            const float4 r4 = SR[4];
+            const int i0 = __float_as_int(r4.x), i1 = __float_as_int(r4.y), i2 = __float_as_int(r4.z);
             const float *Cb = io.colors + (size_t)b * topo.N * 3;
             const float *q0 = Cb + 3 * i0, *q1 = Cb + 3 * i1, *q2 = Cb + 3 * i2;
             col = make_float3(q0[0] * abc.x + q1[0] * abc.y + q2[0] * abc.z, q0[1] * abc.x + q1[1] * abc.y + q2[1] * abc.z,
@@ -449,7 +452,8 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
             col = make_float3((1.0f + n.x) * 0.5f, (1.0f + n.y) * 0.5f, (1.0f + n.z) * 0.5f);
             break;
         case GVR_ALBEDO_TEXTURED_BILINEAR: {
-            const float2 tc = texel_coord(topo.uvs + 6 * (size_t)f, abc, dims.Wt, dims.Ht);
+            const float4 r2 = SR[2], r3 = SR[3];
+            const float2 tc = texel_coord6(r2.y, r2.z, r2.w, r3.x, r3.y, r3.z, abc, dims.Wt, dims.Ht);
             int idx[4];
             float w[4];
             bilinear_taps(tc.x, tc.y, dims.Wt, dims.Ht, idx, w);
@@ -463,8 +467,8 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
             break;
         }
         case GVR_ALBEDO_UV: {
-            const float *t = topo.uvs + 6 * (size_t)f;
-            col = make_float3(abc.x * t[0] + abc.y * t[2] + abc.z * t[4], abc.x * t[1] + abc.y * t[3] + abc.z * t[5],
+            const float4 r2 = SR[2], r3 = SR[3];
+            col = make_float3(abc.x * r2.y + abc.y * r2.w + abc.z * r3.y, abc.x * r2.z + abc.y * r3.x + abc.z * r3.z,
                               0.0f);
             break;
         }
