@@ -5,26 +5,28 @@
 // C[M, N] = A[M, K] * B[N, K]^T (+ bias[N], optional ReLU), A and B
 // row-major with K contiguous ("K-major"), C row-major FP32 or BF16.
 //
-// One CTA of 128 threads computes a 128 x BN tile:
-//   * warp 0 allocates BN columns of tensor memory (128 lanes x BN FP32);
-//   * every K step of 64, all threads copy the A and B tiles from global
-//     memory into shared memory in the canonical no-swizzle K-major layout
-//     (8-row x 16-byte core matrices; core matrices adjacent in K are 128 B
-//     apart, 8-row groups 1024 B apart), fence them to the async proxy and
-//     sync; thread 0 issues four tcgen05.mma (K = 16 each) and a
-//     tcgen05.commit that arrives on the stage's mbarrier when they finish;
-//   * two stages: the copy of step k overlaps the MMAs of step k-1, and a
-//     stage is overwritten only after its mbarrier reports the MMAs that
-//     read it complete;
-//   * the epilogue waits for the last commit, reads the accumulator with
-//     tcgen05.ld (warp w owns lanes 32w..32w+31 = rows), adds the bias,
-//     applies ReLU and stores.
-// Every mbarrier wait is bounded (about one second of %globaltimer) and is
-// done by thread 0 alone; the block then agrees on the outcome with
-// __syncthreads_and, so every thread leaves the K loop, skips the epilogue
-// and reaches the tensor-memory free together.  On timeout the kernel
-// records an error code in g_tc_error, waits once more (bounded) for its
-// MMAs, frees its tensor memory and returns.
+// One CTA of 128 threads computes a 128 x BN tile (BN in {32, 64, 128, 256},
+// the smallest that covers N, else 256) through a pipeline of S stages:
+//   * thread 0 (producer) issues, per K step of 64, two TMA tile loads
+//     (cp.async.bulk.tensor, 128-byte swizzle: rows of 128 B, 16-byte chunks
+//     XOR-permuted within 8-row atoms of 1 KB) into stage s and arms the
+//     stage's `full` mbarrier with their byte count; before reusing a stage
+//     it waits on the stage's `empty` mbarrier;
+//   * thread 32 (MMA issuer) waits on `full`, issues four
+//     tcgen05.mma.cta_group::1.kind::f16 (K = 16 each: the shared-memory
+//     descriptors of the swizzled K-major tiles advance 32 B per K slice)
+//     and a tcgen05.commit that arrives on `empty` when they have read the
+//     stage; after the last step a commit arrives on `done`;
+//   * warp 0 allocates BN columns of tensor memory; after `done`, the four
+//     warps read the accumulator with tcgen05.ld (warp w = TMEM lanes
+//     32w..32w+31 = rows), add the bias, apply ReLU and store 16 bytes at a
+//     time (or add FP32 partials with vector atomics when K is split).
+// Rows and columns outside the matrices are zero-filled by the TMA.  Every
+// mbarrier wait is bounded (about one second of %globaltimer); a timeout
+// sets an error flag in shared memory, the block drains the TMA loads it
+// issued and the MMAs it committed (bounded), skips the epilogue, records
+// the error in g_tc_error, frees its tensor memory and returns.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is looked up at run time)
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -34,8 +36,9 @@
 namespace gvr {
 namespace {
 
-constexpr int kBM = 128, kBK = 64, kThreads = 128, kStages = 2;
-constexpr int kTileBytes = kBM * kBK * 2;  // one 128 x 64 BF16 operand tile (16 KB)
+constexpr int kBM = 128, kBK = 64, kThreads = 128, kMaxStages = 4;
+constexpr int kATileBytes = kBM * kBK * 2;  // one 128 x 64 BF16 operand tile (16 KB)
+constexpr uint64_t kWaitNs = 1000000000ull;
 
 __device__ int g_tc_error;
 
@@ -64,11 +67,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Waits for the phase with `parity` to complete, at most limit_ns (~1 s).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = 1000000000ull) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = kWaitNs) {
     const uint64_t t0 = global_ns();
     while (!mbar_try_wait(bar, parity))
         if (global_ns() - t0 > limit_ns) return false;
     return true;
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// One 2D TMA tile load (x = K element offset, y = row) completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
 }
 
 // Test hook of the bounded waits: one warp waits on an mbarrier that nothing
@@ -85,11 +101,13 @@ __global__ void k_tc_wait_probe(unsigned long long limit_ns) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// Shared-memory matrix descriptor: start address, leading (K) and stride
-// (8-row group) byte offsets, descriptor version 1, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
-           (1ull << 46);
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// start address, leading byte offset 16 (unused for swizzled K-major),
+// stride byte offset 1024 (between 8-row atoms), descriptor version 1,
+// swizzle mode 2 (128 B).  Tiles start on 1 KB boundaries.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(16 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           (1ull << 46) | (2ull << 61);
 }
 
 // Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M x N.
@@ -97,29 +115,19 @@ __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Copies rows [r0, r0 + 128) x K columns [k0, k0 + 64) of a K-major BF16
-// matrix into one canonical tile; rows at or beyond `rows` are zero.
-__device__ __forceinline__ void load_tile(uint8_t *tile, const __nv_bfloat16 *__restrict__ X, int r0, int rows, int k0,
-                                          int ld) {
-    for (int c = threadIdx.x; c < kBM * (kBK / 8); c += kThreads) {
-        const int r = c >> 3, kc = c & 7;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (r0 + r < rows) v = *reinterpret_cast<const uint4 *>(X + (size_t)(r0 + r) * ld + k0 + kc * 8);
-        *reinterpret_cast<uint4 *>(tile + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16) = v;
-    }
-}
-
 template <int BN>
-__global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__restrict__ A,
-                                                        const __nv_bfloat16 *__restrict__ B, void *__restrict__ C,
-                                                        const float *__restrict__ bias, int M, int N, int K, int lda,
-                                                        int ldb, int ldc, int flags) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem;                          // kStages x 16 KB
-    uint8_t *sB = smem + kStages * kTileBytes;   // kStages x (BN x 64 x 2) bytes
-    constexpr int kBTile = BN * kBK * 2;
-    __shared__ __align__(8) uint64_t mbar[kStages];
+__global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __grid_constant__ CUtensorMap tmA,
+                                                        const __grid_constant__ CUtensorMap tmB, void *__restrict__ C,
+                                                        const float *__restrict__ bias, int M, int N, int K, int ldc,
+                                                        int flags, int stages) {
+    constexpr int kBTileBytes = BN * kBK * 2;
+    extern __shared__ uint8_t smemRaw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
+    uint8_t *sA = smem;                         // stages x 16 KB
+    uint8_t *sB = smem + stages * kATileBytes;  // stages x BN x 128 B
+    __shared__ __align__(8) uint64_t fullBar[kMaxStages], emptyBar[kMaxStages], doneBar;
     __shared__ uint32_t tmemBase;
+    __shared__ int sErr, sIssued, sConsumed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
 
@@ -130,8 +138,17 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(&mbar[s], 1);
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(&fullBar[s], 1);
+            mbar_init(&emptyBar[s], 1);
+        }
+        mbar_init(&doneBar, 1);
+        sErr = 0;
+        sIssued = 0;
+        sConsumed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
     }
     tc_fence_before();
     __syncthreads();
@@ -143,37 +160,34 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
     const int KTall = K / kBK, per = (KTall + gridDim.z - 1) / gridDim.z;
     const int ktBegin = blockIdx.z * per, ktEnd = min(KTall, ktBegin + per);
     const int KT = max(0, ktEnd - ktBegin);
-    // The commit of step j arrives on mbar[j % 2]; it completes that
-    // barrier's phase j / 2, so its wait parity is (j / 2) & 1.
-    bool ok = true;
-    int issued = 0;  // steps whose MMAs were committed
-    for (int kt = 0; kt < KT; ++kt) {
-        const int s = kt & 1;
-        if (kt >= kStages) {  // the MMAs of step kt - 2 read this stage
-            bool done = true;
-            if (tid == 0) done = mbar_wait(&mbar[s], ((kt - kStages) >> 1) & 1);
-            if (!__syncthreads_and(done)) {  // one decision for the whole block
-                ok = false;
+
+    if (tid == 0) {  // producer: stage s of round r is free once round r - 1's MMAs have read it
+        int kt = 0;
+        for (; kt < KT; ++kt) {
+            const int s = kt % stages, r = kt / stages;
+            if (r > 0 && !mbar_wait(&emptyBar[s], (r - 1) & 1)) {
+                sErr = 1;
                 break;
             }
+            mbar_arrive_expect_tx(&fullBar[s], (uint32_t)(kATileBytes + kBTileBytes));
+            const int k0 = (ktBegin + kt) * kBK;
+            tma_load_2d(sA + s * kATileBytes, &tmA, &fullBar[s], k0, m0);
+            tma_load_2d(sB + s * kBTileBytes, &tmB, &fullBar[s], k0, n0);
         }
-        const int k0 = (ktBegin + kt) * kBK;
-        load_tile(sA + s * kTileBytes, A, m0, M, k0, lda);
-        for (int c = tid; c < BN * (kBK / 8); c += kThreads) {
-            const int r = c >> 3, kc = c & 7;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (n0 + r < N) v = *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + r) * ldb + k0 + kc * 8);
-            *reinterpret_cast<uint4 *>(sB + s * kBTile + ((r >> 3) * 8 + kc) * 128 + (r & 7) * 16) = v;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+        sIssued = kt;
+    } else if (tid == 32) {  // MMA issuer
+        int kt = 0;
+        for (; kt < KT; ++kt) {
+            const int s = kt % stages, r = kt / stages;
+            if (!mbar_wait(&fullBar[s], r & 1)) {
+                sErr = 1;
+                break;
+            }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + s * kTileBytes), b0 = smem_u32(sB + s * kBTile);
+            const uint32_t a0 = smem_u32(sA + s * kATileBytes), b0 = smem_u32(sB + s * kBTileBytes);
 #pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {  // K = 16 per MMA: two core matrices along K
-                const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
-                const uint64_t bd = smem_desc(b0 + kk * 256, 128, 1024);
+            for (int kk = 0; kk < kBK / 16; ++kk) {  // K = 16 per MMA: 32 B further along the swizzled rows
+                const uint64_t ad = sw128_desc(a0 + kk * 32), bd = sw128_desc(b0 + kk * 32);
                 const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
@@ -183,24 +197,24 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
                     : "memory");
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&mbar[s]))
+                             smem_u32(&emptyBar[s]))
                          : "memory");
         }
-        issued = kt + 1;
+        sConsumed = kt;
+        if (kt > 0)  // tracks every MMA issued before it
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&doneBar))
+                         : "memory");
     }
-    // the last commit tracks every MMA issued before it
-    if (issued > 0) {
-        const int j = issued - 1;
-        bool done = true;
-        if (tid == 0) {
-            done = ok && mbar_wait(&mbar[j & 1], (j >> 1) & 1);
-            if (!done) {  // record, then give the MMAs in flight one more bounded wait before the free
-                atomicExch(&g_tc_error, 1);
-                mbar_wait(&mbar[j & 1], (j >> 1) & 1);
-            }
-        }
-        ok = __syncthreads_and(done) != 0;
+    __syncthreads();
+    bool ok = true;
+    if (tid == 0) {
+        // loads issued but never consumed (only after a timeout) land before the block moves on
+        for (int kt = sConsumed; kt < sIssued; ++kt) mbar_wait(&fullBar[kt % stages], (kt / stages) & 1);
+        ok = (sConsumed == 0 || mbar_wait(&doneBar, 0)) && sErr == 0;
+        if (!ok) atomicExch(&g_tc_error, 1);
     }
+    ok = __syncthreads_and(ok) != 0;
     tc_fence_after();
 
     if (ok && KT > 0) {
@@ -208,6 +222,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
         const bool relu = flags & GVR_GEMM_RELU, outBf16 = flags & GVR_GEMM_OUT_BF16;
         const bool split = gridDim.z > 1, addBias = bias && blockIdx.z == 0;
+        const bool vec = (ldc % 8) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0;
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 16) {
             uint32_t v[16];
@@ -219,20 +234,47 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16(const __nv_bfloat16 *__r
                   "=r"(v[15])
                 : "r"(taddr + (uint32_t)c0));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < M) {
+            const int col0 = n0 + c0;
+            if (row >= M || col0 >= N) continue;
+            float x[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int col = n0 + c0 + j;
-                    if (col >= N) break;
-                    float x = __uint_as_float(v[j]);
-                    if (addBias) x += bias[col];
-                    if (split) {
-                        atomicAdd(reinterpret_cast<float *>(C) + (size_t)row * ldc + col, x);
-                        continue;
+            for (int j = 0; j < 16; ++j) {
+                x[j] = __uint_as_float(v[j]);
+                if (addBias && col0 + j < N) x[j] += bias[col0 + j];
+                if (!split && relu) x[j] = fmaxf(x[j], 0.0f);
+            }
+            const bool full = col0 + 16 <= N && vec;
+            if (split) {
+                float *Cr = reinterpret_cast<float *>(C) + (size_t)row * ldc + col0;
+                if (full) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        atomicAdd(reinterpret_cast<float4 *>(Cr) + q, make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]));
+                } else {
+                    for (int j = 0; j < 16 && col0 + j < N; ++j) atomicAdd(Cr + j, x[j]);
+                }
+            } else if (outBf16) {
+                __nv_bfloat16 *Cr = reinterpret_cast<__nv_bfloat16 *>(C) + (size_t)row * ldc + col0;
+                if (full) {
+                    uint32_t w[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(x[2 * q], x[2 * q + 1]);
+                        w[q] = *reinterpret_cast<const uint32_t *>(&h);
                     }
-                    if (relu) x = fmaxf(x, 0.0f);
-                    if (outBf16) reinterpret_cast<__nv_bfloat16 *>(C)[(size_t)row * ldc + col] = __float2bfloat16_rn(x);
-                    else reinterpret_cast<float *>(C)[(size_t)row * ldc + col] = x;
+                    reinterpret_cast<uint4 *>(Cr)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                    reinterpret_cast<uint4 *>(Cr)[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                } else {
+                    for (int j = 0; j < 16 && col0 + j < N; ++j) Cr[j] = __float2bfloat16_rn(x[j]);
+                }
+            } else {
+                float *Cr = reinterpret_cast<float *>(C) + (size_t)row * ldc + col0;
+                if (full) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        reinterpret_cast<float4 *>(Cr)[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+                } else {
+                    for (int j = 0; j < 16 && col0 + j < N; ++j) Cr[j] = x[j];
                 }
             }
         }
@@ -287,20 +329,69 @@ __global__ void k_col2im_3x3s2(const float *__restrict__ col, float *__restrict_
     dx[i] = acc;
 }
 
-template <int BN>
-cudaError_t launch_gemm(const GvrGemmArgs &a, cudaStream_t st) {
-    const int smem = kStages * (kTileBytes + BN * kBK * 2);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link-time
+// dependency on the driver library).
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
     }
-    dim3 grid((a.N + BN - 1) / BN, (a.M + kBM - 1) / kBM, a.k_splits > 1 ? a.k_splits : 1);
-    GVR_LAUNCH(st, BN == 128 ? "k_gemm_bf16_n128" : "k_gemm_bf16_n64",
-               (k_gemm_bf16<BN><<<grid, kThreads, smem, st>>>(
-                   static_cast<const __nv_bfloat16 *>(a.A), static_cast<const __nv_bfloat16 *>(a.B), a.C, a.bias,
-                   a.M, a.N, a.K, a.lda, a.ldb, a.ldc, a.flags)));
+    return fn;
+}
+
+// Tensor map of a row-major BF16 matrix [rows, K] with row stride ld
+// elements, read in boxes of `boxRows` rows x 64 K-elements (128 B) with
+// 128-byte swizzle; out-of-range rows read as zeros.
+bool make_map(CUtensorMap *map, const void *base, int rows, int K, int ld, int boxRows) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)boxRows};
+    const cuuint32_t elem[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, elem,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+cudaError_t launch_gemm(const GvrGemmArgs &a, cudaStream_t st, bool &mapFailed) {
+    constexpr int stageBytes = kATileBytes + BN * kBK * 2;
+    // about 100 KB of stages in flight per CTA (two CTAs per SM), 2..4 deep,
+    // no deeper than this CTA's K steps
+    const int KTall = a.K / kBK, splits = a.k_splits > 1 ? a.k_splits : 1;
+    const int per = (KTall + splits - 1) / splits;
+    const int stages = max(1, min(min(kMaxStages, max(2, (100 * 1024) / stageBytes)), per));
+    // + alignment slack for the 1 KB swizzle atoms; at least enough that no
+    // more CTAs fit on an SM than its 512 tensor-memory columns hold
+    constexpr int kSmemPerSM = 233472, kTmemCols = 512;
+    const int smem = max(stages * stageBytes + 1024, kSmemPerSM / (kTmemCols / BN + 1) - 1024 + 16);
+    static int attrBytes = 0;
+    if (smem > attrBytes) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kMaxStages * stageBytes + 1024);
+        if (e != cudaSuccess) return e;
+        attrBytes = kMaxStages * stageBytes + 1024;
+    }
+    CUtensorMap mA, mB;
+    if (!make_map(&mA, a.A, a.M, a.K, a.lda, kBM) || !make_map(&mB, a.B, a.N, a.K, a.ldb, BN)) {
+        mapFailed = true;
+        return cudaErrorInvalidValue;
+    }
+    dim3 grid((a.N + BN - 1) / BN, (a.M + kBM - 1) / kBM, splits);
+    GVR_LAUNCH(st, BN == 256 ? "k_gemm_bf16_n256" : BN == 128 ? "k_gemm_bf16_n128" : BN == 64 ? "k_gemm_bf16_n64"
+                                                                                               : "k_gemm_bf16_n32",
+               (k_gemm_bf16<BN><<<grid, kThreads, smem, st>>>(mA, mB, a.C, a.bias, a.M, a.N, a.K, a.ldc, a.flags,
+                                                               stages)));
     return cudaGetLastError();
 }
 
@@ -330,8 +421,15 @@ int gvr_gemm_bf16(const GvrGemmArgs *a, void *stream) {
     if ((long long)(a->M + 127) / 128 > 65535) return nn_fail(GVR_ERR_INVALID_ARGUMENT, "gemm: M too large");
     if (a->k_splits > 1 && (a->k_splits > 65535 || (a->flags & (GVR_GEMM_RELU | GVR_GEMM_OUT_BF16))))
         return nn_fail(GVR_ERR_INVALID_ARGUMENT, "gemm: k_splits needs FP32 output without ReLU (and <= 65535)");
+    if ((long long)(a->N + 255) / 256 > 2147483647LL || a->M > 2147483647 - 127)
+        return nn_fail(GVR_ERR_INVALID_ARGUMENT, "gemm: N or M too large");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaError_t e = a->N <= 64 ? gvr::launch_gemm<64>(*a, st) : gvr::launch_gemm<128>(*a, st);
+    bool mapFailed = false;
+    const cudaError_t e = a->N <= 32    ? gvr::launch_gemm<32>(*a, st, mapFailed)
+                          : a->N <= 64  ? gvr::launch_gemm<64>(*a, st, mapFailed)
+                          : a->N <= 128 ? gvr::launch_gemm<128>(*a, st, mapFailed)
+                                        : gvr::launch_gemm<256>(*a, st, mapFailed);
+    if (mapFailed) return nn_fail(GVR_ERR_CUDA, "gemm: tensor map encoding failed (cuTensorMapEncodeTiled)");
     return e == cudaSuccess ? GVR_OK : nn_fail(GVR_ERR_CUDA, cudaGetErrorString(e));
 }
 

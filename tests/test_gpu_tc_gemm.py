@@ -18,7 +18,8 @@ def _rel(a, b):
     return float((a - b).abs().max() / b.abs().max().clamp_min(1e-30))
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 200, 192), (1000, 64, 576), (77, 193, 512), (4096, 256, 2304)])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 200, 192), (1000, 64, 576), (77, 193, 512), (4096, 256, 2304),
+                                   (4096, 32, 64), (513, 1000, 128), (260, 2304, 320), (129, 48, 4096)])
 def test_gemm_matches_fp32_reference(M, N, K):
     import torch
     from gvr import tc
