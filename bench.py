@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--fits", type=int, default=1000, help="held-out seeds of the fit / learned workloads")
     ap.add_argument("--train-renders", type=int, default=1_000_000, help="renders the proposal network trains on")
     ap.add_argument("--fit-batch", type=int, default=50, help="fits run together")
+    ap.add_argument("--gemm-shapes", default="", help="gemm workload: comma-separated shape names to run (default all)")
     return ap.parse_args()
 
 
@@ -694,6 +695,9 @@ def run_gemm_bench(args):
         shapes.append((f"conv{i + 1} wgrad", co, K, M, torch.float32))
     shapes += [("fc1 fwd", B, 1024, 16384, torch.float32), ("fc1 dgrad", B, 16384, 1024, torch.float32),
                ("fc1 wgrad", 1024, 16384, B, torch.float32), ("fc2 fwd", B, 193, 1024, torch.float32)]
+    if args.gemm_shapes:
+        keep = {x.strip() for x in args.gemm_shapes.split(",")}
+        shapes = [sh for sh in shapes if sh[0] in keep]
     peaks = {}
     pk = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(pk):

@@ -6,8 +6,10 @@ oracle must reproduce the reference bit for bit: face ids on every pixel
 whose minimal quantised depth is unique (elsewhere the reference's write
 race picks one of the tied faces), barycentrics and vertex normals.  Render
 values: 1e-5 relative (the oracle is FP64).  Gradients: colour, texture and
-SH 1e-4 relative; positions 2e-2 (the reference's FP32 Jacobians lose
-accuracy at grazing incidence, the FP64 oracle does not).
+SH 1e-4 relative; positions 2e-2 on all pixels (the reference's FP32
+Jacobians lose accuracy at grazing incidence, the FP64 oracle does not) and
+1e-4 on the *_interior fixtures, whose upstream gradients are zero off the
+well-conditioned pixels (tests/helpers.py interior_mask).
 """
 import glob
 import os
@@ -47,7 +49,10 @@ def test_oracle_reproduces_reference_kernels(path):
                 assert np.all(z["ref_" + k] == 0), k
             else:
                 assert rel_norm(z["ref_" + k], g[k]) < 1e-4, k
-        assert rel_norm(z["ref_vertex_pos_grad"], g["vertex_pos_grad"]) < 2e-2
+        # all pixels: the reference's FP32 Jacobians lose accuracy at grazing incidence;
+        # interior fixtures (grad_render zero elsewhere): the full parity bar
+        bar = 1e-4 if ("interior" in z and bool(z["interior"])) else 2e-2
+        assert rel_norm(z["ref_vertex_pos_grad"], g["vertex_pos_grad"]) < bar
 
 
 UV_FIXTURES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "uvmap", "*.npz")))
