@@ -626,6 +626,8 @@ def run_fit_bench(args):
     dev = torch.device("cuda", local)
     from gvr import fitting, native_build, proposal, tc
     native_build.build()
+    clocks = ClockSampler(local)
+    clocks.start()
     model = fitting.MorphableModel(num_vertices=28000, seed=0, device=dev)
     fitter = fitting.Fitter(model, num_views=4, size=512, silhouette=fitting.Fitter.SILHOUETTE)
     seeds = list(range(1_000_000, 1_000_000 + args.fits))
@@ -661,6 +663,7 @@ def run_fit_bench(args):
                                                    if ps["gpu_ms_per_fit_reaching_goal"] and
                                                    ls["gpu_ms_per_fit_reaching_goal"] else None),
                     training={"steps": steps, "seconds": secs, "loss": losses, "tc_error": tc.tc_error()})
+    line["clocks"] = clocks.stop()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
