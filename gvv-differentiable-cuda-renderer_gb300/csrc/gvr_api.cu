@@ -89,6 +89,7 @@ void fwd_carve_main(const GvrHandle *h, int B, int Ht, int Wt, const TileCfg &tc
     L.s.cams = c.take<gvr::Camera>(BC);
     L.s.geo = c.take<gvr::FaceGeo>((size_t)B * h->F);
     L.s.fnormal = c.take<float4>((size_t)B * h->F);
+    L.s.faceC = c.take<float4>((size_t)B * h->F);
     L.proj = c.take<float4>(BC * h->N);
     if (h->attrs.compute_normal_map) {  // no binning: the depth and shading passes do not run
         L.uvOwner = c.take<int>((size_t)(Ht > 0 ? Ht : 1) * (Wt > 0 ? Wt : 1));

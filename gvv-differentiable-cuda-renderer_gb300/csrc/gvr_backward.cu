@@ -682,10 +682,23 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     }
     const bool shaded = backward_shaded(dims.albedo, dims.shading);
     const bool target = a.target_grad != nullptr;
-    if ((err = cudaMemsetAsync(ws.faceAcc, 0, (size_t)B * F * kFaceAccFloats * sizeof(float), st))) return err;
-    if ((err = cudaMemsetAsync(a.texture_grad, 0, texBytes, st))) return err;
-    if ((err = launch_cameras(a.extrinsics, a.intrinsics, ws.cams, B * C, st))) return err;
-    if ((err = launch_face_geo(a.vertex_pos, topo, ws.geo, nullptr, B, st, ws.faceRec))) return err;
+    SetupArgs sa{};  // cameras, face records, cleared face accumulators and texture gradient: one launch
+    sa.verts = a.vertex_pos;
+    sa.faces = topo.faces;
+    sa.uvs = topo.uvs;
+    sa.N = N;
+    sa.F = F;
+    sa.B = B;
+    sa.geo = ws.geo;
+    sa.rec = ws.faceRec;
+    sa.faceAcc = ws.faceAcc;
+    sa.extr = a.extrinsics;
+    sa.intr = a.intrinsics;
+    sa.cams = ws.cams;
+    sa.views = B * C;
+    sa.zero = a.texture_grad;
+    sa.zeroWords = (long long)(texBytes / sizeof(float));
+    if ((err = launch_setup(sa, st))) return err;
     const int phong = dims.shading == GVR_SHADING_PHONG && dims.albedo != GVR_ALBEDO_FOREGROUND_MASK;
     BwdIO io{a.render_grad, a.vertex_pos, a.vertex_color, a.texture, a.sh_coeff, a.target_image, a.vertex_normal,
              a.barycentric, a.face, a.target_grad, a.texture_grad, imageFilter, phong};

@@ -109,6 +109,7 @@ __device__ __forceinline__ void camera_item(const float *__restrict__ extr, cons
 #pragma unroll
     for (int j = 0; j < 3; ++j) cam.origS[j] = xd(cam.orig[j], 1000.0f);
     cam.origS[3] = 0.0f;
+    cam.origLen = sqrtf(cam.orig[0] * cam.orig[0] + cam.orig[1] * cam.orig[1] + cam.orig[2] * cam.orig[2]);
 #pragma unroll
     for (int j = 0; j < 12; ++j) { cam.KE[j] = KE[j]; cam.E[j] = e12[j]; }
 #pragma unroll
@@ -122,7 +123,8 @@ __device__ __forceinline__ void camera_item(const float *__restrict__ extr, cons
 __device__ __forceinline__ void face_geo_item(const float *__restrict__ verts, const int32_t *__restrict__ faces,
                                               FaceGeo *__restrict__ geo, float4 *__restrict__ fnormal, int N, int F,
                                               int i, float4 *__restrict__ rec = nullptr,
-                                              const float *__restrict__ uvs = nullptr) {
+                                              const float *__restrict__ uvs = nullptr,
+                                              float4 *__restrict__ faceC = nullptr) {
     int b = i / F, f = i - b * F;
     const float *V = verts + (size_t)b * N * 3;
     int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
@@ -139,7 +141,16 @@ __device__ __forceinline__ void face_geo_item(const float *__restrict__ verts, c
         R[4] = make_float4(p2.y, p2.z, 0.0f, 0.0f);
     }
     V3 fn = xcross(xsub(p1, p0), xsub(p2, p0));
-    if (fnormal) fnormal[i] = make_float4(fn.x, fn.y, fn.z, 0.0f);
+    const float fnLen = sqrtf(fn.x * fn.x + fn.y * fn.y + fn.z * fn.z);
+    if (fnormal) fnormal[i] = make_float4(fn.x, fn.y, fn.z, fnLen);
+    if (faceC) {  // what the binning pass's skip-test margins need of the face, whatever the view
+        auto elen = [](V3 a, V3 c) {
+            return sqrtf((a.x - c.x) * (a.x - c.x) + (a.y - c.y) * (a.y - c.y) + (a.z - c.z) * (a.z - c.z));
+        };
+        const float maxEdge = fmaxf(elen(p0, p1), fmaxf(elen(p1, p2), elen(p2, p0)));
+        faceC[i] = make_float4((p0.x + p1.x + p2.x) * (1.0f / 3.0f), (p0.y + p1.y + p2.y) * (1.0f / 3.0f),
+                               (p0.z + p1.z + p2.z) * (1.0f / 3.0f), fnLen / maxEdge);
+    }
     // rayTriangleIntersect scales vertices by 1/1000 (RendererUtil.h:29-32)
     V3 s0 = v3(xd(p0.x, 1000.0f), xd(p0.y, 1000.0f), xd(p0.z, 1000.0f));
     V3 s1 = v3(xd(p1.x, 1000.0f), xd(p1.y, 1000.0f), xd(p1.z, 1000.0f));
@@ -223,24 +234,17 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
     const float ex1 = p1.x - p0.x, ey1 = p1.y - p0.y, ex2 = p2.x - p0.x, ey2 = p2.y - p0.y;
     const float det = ex1 * ey2 - ey1 * ex2;
     const float zmn = fminf(p0.z, fminf(p1.z, p2.z)), zmx = fmaxf(p0.z, fmaxf(p1.z, p2.z));
-    const float *V = J.io.verts + (size_t)b * N * 3;
     const Camera &cam = ws.cams[bc];
-    const float4 fn = ws.fnormal[(size_t)b * F + f];
-    const V3 w0 = ld3(V + 3 * i0), w1 = ld3(V + 3 * i1), w2 = ld3(V + 3 * i2);
-    const float cx = (w0.x + w1.x + w2.x) * (1.0f / 3.0f), cy = (w0.y + w1.y + w2.y) * (1.0f / 3.0f),
-                cz = (w0.z + w1.z + w2.z) * (1.0f / 3.0f);
+    const float4 fn = ws.fnormal[(size_t)b * F + f];  // w: its length
+    const float4 fc = ws.faceC[(size_t)b * F + f];    // centroid, smallest altitude (mm)
+    const float cx = fc.x, cy = fc.y, cz = fc.z, alt = fc.w, fnLen = fn.w;
     const float vx = cx - cam.orig[0], vy = cy - cam.orig[1], vz = cz - cam.orig[2];
     const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
-    const float fnLen = sqrtf(fn.x * fn.x + fn.y * fn.y + fn.z * fn.z);
     const float cosv = fabsf(fn.x * vx + fn.y * vy + fn.z * vz) / (fnLen * dist);
-    auto elen = [](V3 a, V3 c) { return sqrtf((a.x - c.x) * (a.x - c.x) + (a.y - c.y) * (a.y - c.y) + (a.z - c.z) * (a.z - c.z)); };
-    const float maxEdge = fmaxf(elen(w0, w1), fmaxf(elen(w1, w2), elen(w2, w0)));
-    const float alt = fnLen / maxEdge;  // smallest altitude, mm
     const float sEdge = fmaxf(sqrtf(ex1 * ex1 + ey1 * ey1), fmaxf(sqrtf(ex2 * ex2 + ey2 * ey2),
                               sqrtf((p2.x - p1.x) * (p2.x - p1.x) + (p2.y - p1.y) * (p2.y - p1.y))));
     const float altPx = fabsf(det) / sEdge;  // smallest screen altitude, pixels
-    const float scale = sqrtf(cam.orig[0] * cam.orig[0] + cam.orig[1] * cam.orig[1] + cam.orig[2] * cam.orig[2]) +
-                        sqrtf(cx * cx + cy * cy + cz * cz) + dist;
+    const float scale = cam.origLen + sqrtf(cx * cx + cy * cy + cz * cz) + dist;
     const bool valid = zmn >= 1.0f && zmx <= 64.0f * zmn && fabsf(det) > 1e-6f && isfinite(det) &&
                        isfinite(p0.x + p1.x + p2.x + p0.y + p1.y + p2.y) && isfinite(cosv) && alt > 0.0f;
     int flags = 0;
@@ -469,7 +473,9 @@ __global__ void __launch_bounds__(kBatchBlock) k_stage_batched(const FwdJob *__r
     const int i = (blockIdx.x - blockStart[j]) * kBatchBlock + threadIdx.x;
     if (i >= stage_count(J, STAGE)) return;
     if (STAGE == kStageViews) camera_item(J.extr, J.intr, J.ws.cams, i);
-    else if (STAGE == kStageFaces) face_geo_item(J.io.verts, J.topo.faces, J.ws.geo, J.ws.fnormal, J.topo.N, J.topo.F, i);
+    else if (STAGE == kStageFaces)
+        face_geo_item(J.io.verts, J.topo.faces, J.ws.geo, J.ws.fnormal, J.topo.N, J.topo.F, i, nullptr, nullptr,
+                      J.ws.faceC);
     else if (STAGE == kStageVertices) vertex_item(J, i);
     else if (STAGE == kStageBinCount) bin_count_item(J, i);
     else bin_fill_item(J, i);
@@ -496,9 +502,51 @@ __global__ void __launch_bounds__(1024) k_scan_tiles_batched(const FwdJob *__res
     scan_block(J.ws.tileCount, J.ws.tileStart, J.dims.B * J.dims.C * J.dims.tilesX * J.dims.tilesY);
 }
 
+// The set-up of one call in one launch: the face pass (scaled geometry, face
+// normals, and in the backward the face records and the cleared face
+// accumulators), the camera records and a cleared region (the forward's
+// per-call counters, or the backward's texture gradient).  Threads
+// [0, faces) take faces, the next `views` take cameras, the rest clear.
+__global__ void k_setup(const SetupArgs A) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nF = (long long)A.B * A.F;
+    if (i < nF) {
+        face_geo_item(A.verts, A.faces, A.geo, A.fnormal, A.N, A.F, (int)i, A.rec, A.uvs, A.faceC);
+        if (A.faceAcc) {
+            float4 *acc = A.faceAcc + i * (kFaceAccFloats / 4);
+#pragma unroll
+            for (int q = 0; q < kFaceAccFloats / 4; ++q) acc[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        return;
+    }
+    const long long c = i - nF;
+    if (c < A.views) {
+        camera_item(A.extr, A.intr, A.cams, (int)c);
+        return;
+    }
+    const long long z = c - A.views;  // four words per thread when the region is 16-byte aligned, else one
+    float *w = reinterpret_cast<float *>(A.zero);
+    if (A.zeroVec) {
+        if (4 * z + 3 < A.zeroWords) reinterpret_cast<float4 *>(w)[z] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        else
+            for (long long k = 4 * z; k < A.zeroWords; ++k) w[k] = 0.0f;
+    } else if (z < A.zeroWords) {
+        w[z] = 0.0f;
+    }
+}
+
 // ---------------------------------------------------------------------------- host launch
 
 static inline int blocks(size_t n, int t) { return (int)((n + t - 1) / t); }
+
+cudaError_t launch_setup(SetupArgs a, cudaStream_t st) {
+    a.zeroVec = ((reinterpret_cast<uintptr_t>(a.zero) & 15) == 0) ? 1 : 0;
+    const long long zt = a.zero ? (a.zeroVec ? (a.zeroWords + 3) / 4 : a.zeroWords) : 0;
+    const long long n = (long long)a.B * a.F + a.views + zt;
+    if (n == 0) return cudaSuccess;
+    GVR_LAUNCH(st, "k_setup", k_setup<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a));
+    return cudaGetLastError();
+}
 
 cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, int count, cudaStream_t st) {
     GVR_LAUNCH(st, "k_cameras", k_cameras<<<blocks(count, 64), 64, 0, st>>>(extr, intr, cams, count));
@@ -521,10 +569,24 @@ static cudaError_t launch_vertices(const FwdJob &J, cudaStream_t st) {
 cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
     const FrameDims &dims = J.dims;
     const int B = dims.B, C = dims.C, T = dims.tilesX * dims.tilesY;
-    cudaError_t err = cudaMemsetAsync(J.ws.zeroBase, 0, J.ws.zeroBytes, st);
+    SetupArgs sa{};
+    sa.verts = J.io.verts;
+    sa.faces = J.topo.faces;
+    sa.uvs = J.topo.uvs;
+    sa.N = J.topo.N;
+    sa.F = J.topo.F;
+    sa.B = B;
+    sa.geo = J.ws.geo;
+    sa.fnormal = J.ws.fnormal;
+    sa.faceC = J.ws.faceC;
+    sa.extr = J.extr;
+    sa.intr = J.intr;
+    sa.cams = J.ws.cams;
+    sa.views = B * C;
+    sa.zero = J.ws.zeroBase;
+    sa.zeroWords = (long long)(J.ws.zeroBytes / 4);
+    cudaError_t err = launch_setup(sa, st);
     if (err != cudaSuccess) return err;
-    if ((err = launch_cameras(J.extr, J.intr, J.ws.cams, B * C, st)) != cudaSuccess) return err;
-    if ((err = launch_face_geo(J.io.verts, J.topo, J.ws.geo, J.ws.fnormal, B, st)) != cudaSuccess) return err;
     if ((err = launch_vertices(J, st)) != cudaSuccess) return err;
     const size_t nvf = (size_t)B * C * J.topo.F;
     GVR_LAUNCH(st, "k_bin_count", k_bin_count<<<blocks(nvf, 256), 256, 0, st>>>(J));

@@ -53,7 +53,8 @@ struct Camera {
     float KE[12];     // K*E (3x4), used by the target-image Jacobian
     float K[9];       // intrinsics
     float E[12];      // extrinsics
-    float pad[59];    // 128 floats = 512 B
+    float origLen;    // |orig|, mm (the skip tests' error scale)
+    float pad[58];    // 128 floats = 512 B
 };
 
 // Per (batch, face) geometry in the reference's scaled units (/1000).
@@ -329,7 +330,8 @@ constexpr int kShadeRows = 5;
 struct FwdScratch {
     Camera *cams;        // [B*C]
     FaceGeo *geo;        // [B*F]
-    float4 *fnormal;     // [B*F] un-normalised face normals
+    float4 *fnormal;     // [B*F] un-normalised face normals; w = their length
+    float4 *faceC;       // [B*F] centroid (mm) and smallest altitude (mm) of each face
     float4 *shadeRec;    // [B*F*kShadeRows], written by the binning pass
     ViewFace *vface;     // [B*C*F]
     int *tileCount;      // [B*C*T]

@@ -59,6 +59,26 @@ struct BwdBatchLaunch {
 // The pixel-kernel variant of a backward call, or -1 for the zero-gradient modes.
 int backward_variant(int albedo, int shading, bool target, bool albpos);
 
+// One call's set-up in one launch (k_setup): face pass, camera records and
+// a region cleared to zero.
+struct SetupArgs {
+    const float *verts;       // [B,N,3]
+    const int32_t *faces;     // [F*3]
+    const float *uvs;         // [F*6] (the backward's face records) or null
+    int N, F, B;
+    FaceGeo *geo;             // [B*F]
+    float4 *fnormal;          // [B*F] or null
+    float4 *faceC;            // [B*F] centroid and smallest altitude (the forward's skip tests), or null
+    float4 *rec;              // [B*F*kBwdFaceRows] backward face records, or null
+    float4 *faceAcc;          // [B*F*kFaceAccFloats/4] cleared, or null
+    const float *extr, *intr; // [views,12], [views,9]
+    Camera *cams;             // [views]
+    int views;
+    void *zero;               // region cleared (zeroWords 4-byte words), or null
+    long long zeroWords;
+    int zeroVec;              // set by the launcher: the region is 16-byte aligned
+};
+cudaError_t launch_setup(SetupArgs a, cudaStream_t st);
 cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, int count, cudaStream_t st);
 cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *geo, float4 *fnormal, int B,
                             cudaStream_t st, float4 *bwdRec = nullptr);

@@ -375,12 +375,16 @@ cudaError_t launch_gemm(const GvrGemmArgs &a, cudaStream_t st, bool &mapFailed) 
     // more CTAs fit on an SM than its 512 tensor-memory columns hold
     constexpr int kSmemPerSM = 233472, kTmemCols = 512;
     const int smem = max(stages * stageBytes + 1024, kSmemPerSM / (kTmemCols / BN + 1) - 1024 + 16);
-    static int attrBytes = 0;
-    if (smem > attrBytes) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kMaxStages * stageBytes + 1024);
+    // the kernel's shared-memory limit is a per-device attribute: raise it once per device
+    static bool raised[64] = {false};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64 || !raised[dev]) {
+        e = cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kMaxStages * stageBytes + 1024);
         if (e != cudaSuccess) return e;
-        attrBytes = kMaxStages * stageBytes + 1024;
+        if (dev >= 0 && dev < 64) raised[dev] = true;
     }
     CUtensorMap mA, mB;
     if (!make_map(&mA, a.A, a.M, a.K, a.lda, kBM) || !make_map(&mB, a.B, a.N, a.K, a.ldb, BN)) {
