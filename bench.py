@@ -80,8 +80,8 @@ def kernel_bytes(name, P, C, N, F, Ht, Wt, textured, target):
     """Algorithmic bytes of one launch of the two pixel kernels."""
     if name == "k_raster":    # render 12 + face 4 + bary 8 per pixel; vertex normals, faces, uvs, texture read
         return P * 24 + C * (12 * N + 12 * F + 24 * F * textured) + 12 * Ht * Wt * textured
-    if name == "k_bwd_pixels":  # grad_render 12 + face 4 (+ target and its grad) per pixel; texture grad written
-        return P * (16 + 24 * target) + C * (12 * N + 12 * F + 24 * F * textured) + 24 * Ht * Wt * textured
+    if name == "k_bwd_pixels":  # grad_render 12 + face 4 + bary 8 (+ target and its grad) per pixel; texture grad written
+        return P * (24 + 24 * target) + C * (12 * N + 12 * F + 24 * F * textured) + 24 * Ht * Wt * textured
     return None
 
 
@@ -301,7 +301,7 @@ def run_gvr(args):
                              None, p(d["extrinsics"]), p(d["intrinsics"]), p(out["bary"]), p(out["face"]),
                              p(out["render"]), p(out["vnorm"]), None, None, p(fws), fws.numel())
     ba = _lib.GvrBackwardArgs(B, Ht, Wt, p(d["grad_render"]), p(d["vertex_pos"]), p(d["vertex_color"]), p(d["texture"]),
-                              p(d["sh_coeff"]), None, p(out["vnorm"]), None, p(out["face"]), None, p(d["extrinsics"]),
+                              p(d["sh_coeff"]), None, p(out["vnorm"]), p(out["bary"]), p(out["face"]), None, p(d["extrinsics"]),
                               p(d["intrinsics"]), p(out["gpos"]), p(out["gcol"]), p(out["gtex"]), p(out["gsh"]),
                               p(bws), bws.numel())
     stream = torch.cuda.current_stream(dev)
@@ -387,7 +387,7 @@ def run_gvr(args):
                                        p(dd["sh_coeff"]), None, p(dd["extrinsics"]), p(dd["intrinsics"]), p(oo["bary"]),
                                        p(oo["face"]), p(oo["render"]), p(oo["vnorm"]), None, None, p(fws), fws.numel()))
         bas.append(_lib.GvrBackwardArgs(B, Ht, Wt, p(dd["grad_render"]), p(dd["vertex_pos"]), p(dd["vertex_color"]),
-                                        p(dd["texture"]), p(dd["sh_coeff"]), None, p(oo["vnorm"]), None, p(oo["face"]),
+                                        p(dd["texture"]), p(dd["sh_coeff"]), None, p(oo["vnorm"]), p(oo["bary"]), p(oo["face"]),
                                         None, p(dd["extrinsics"]), p(dd["intrinsics"]), p(oo["gpos"]), p(oo["gcol"]),
                                         p(oo["gtex"]), p(oo["gsh"]), p(bws), bws.numel()))
     s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)

@@ -4,9 +4,11 @@
 // Reference: renderBuffersGradDevice (cpp/src/Renderer/CUDABasedRasterizationGrad.cu:114-617),
 // one thread per pixel issuing ~210 float atomics per covered pixel.  Here:
 //
-//  k_bwd_pixels  one thread per pixel of a 16x16 tile.  Barycentrics are
-//                recomputed from the face-id buffer with the forward's exact
-//                FP32 ray/triangle arithmetic.  Per pixel the chain rule gives
+//  k_bwd_pixels  one thread per pixel of a 16x16 tile.  Barycentrics come
+//                from the forward's barycentric buffer, as the reference reads
+//                them (without one they are recomputed from the face id with
+//                the forward's exact FP32 ray/triangle test).  Per pixel the
+//                chain rule gives
 //                three 3-vectors weighted by the barycentric of each corner j:
 //                  pos_j = b_j * (m - q)   shading + target-image terms
 //                  gN_j  = b_j * w         d(loss)/d(un-normalised vertex normal)
@@ -127,28 +129,31 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
     }
     int f = inImage ? io.face[p] : -1;
     if (f >= F) f = -1;  // ids outside [0, F) carry no face
+    // the forward's barycentrics, as the reference's grad reads them
+    // (CUDABasedRasterizationGrad.cu:210-211); loaded alongside the face id
+    const float2 bIn = inImage && io.bary_in ? reinterpret_cast<const float2 *>(io.bary_in)[p] : make_float2(0.0f, 0.0f);
     __syncthreads();
-    float val[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) val[k] = 0.0f;
     float shv[SHADED ? 32 : 1];  // 27 SH terms, padded to a warp for the reduce-scatter
 #pragma unroll
     for (int k = 0; k < (SHADED ? 32 : 1); ++k) shv[k] = 0.0f;
+    // what the position terms take from the shading phase: the ray, the
+    // barycentrics, wv = d(loss)/d(un-normalised normal), rr[j] = d(loss)/d(b_j)
+    // of the shading term and the colour weight gl = G * light
+    V3 d = v3(0.0f, 0.0f, 0.0f), abc = v3(0.0f, 0.0f, 0.0f);
+    float wv[3] = {0.0f, 0.0f, 0.0f}, rr[3] = {0.0f, 0.0f, 0.0f}, gl[3] = {0.0f, 0.0f, 0.0f};
 
+    // ---- shading phase: normal, albedo and light; texel, SH and colour terms
     if (f >= 0) {
         const Camera &cam = sCam;
-        const V3 origS = v3(cam.origS[0], cam.origS[1], cam.origS[2]);
-        const V3 d = pixel_ray(cam, u, v);
-        const FaceSetup fs = load_face(&ws.geo[(size_t)b * F + f]);
-        V3 abc = barycentric(fs, origS, xdot(origS, fs.n), d);
-        if (abc.x == -1.0f && abc.y == -1.0f && abc.z == -1.0f) {
-            // face buffer inconsistent with the geometry: fall back to the stored barycentrics
-            if (io.bary_in) {
-                float2 bb = reinterpret_cast<const float2 *>(io.bary_in)[p];
-                abc = v3(bb.x, bb.y, xs(xs(1.0f, bb.x), bb.y));
-            } else {
-                f = -1;
-            }
+        d = pixel_ray(cam, u, v);
+        abc = v3(bIn.x, bIn.y, xs(xs(1.0f, bIn.x), bIn.y));
+        if (!io.bary_in) {
+            // no barycentric buffer: recompute them from the face id with the
+            // forward's exact test (a face the ray misses contributes nothing)
+            const V3 origS = v3(cam.origS[0], cam.origS[1], cam.origS[2]);
+            const FaceSetup fs = load_face(&ws.geo[(size_t)b * F + f]);
+            abc = barycentric(fs, origS, xdot(origS, fs.n), d);
+            if (abc.x == -1.0f && abc.y == -1.0f && abc.z == -1.0f) f = -1;
         }
         if (f >= 0) {
             const float4 *FR = ws.faceRec + ((size_t)b * F + f) * kBwdFaceRows;  // the face's record
@@ -222,16 +227,8 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                               w[k] * (G[2] * JCoAl[2]));
                 }
             }
-            // Pv: per-pixel vector applied with the stored barycentrics (target term);
-            // Qv[j]: shading term already weighted for corner j
-            float Pv[3] = {0.0f, 0.0f, 0.0f}, wv[3] = {0.0f, 0.0f, 0.0f}, rr[3] = {0.0f, 0.0f, 0.0f};
-            float Qv[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
             if (SHADED) {
                 const float ga[3] = {G[0] * alb[0], G[1] * alb[1], G[2] * alb[2]};
-#pragma unroll
-                for (int ch = 0; ch < 3; ++ch)
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) shv[9 * ch + k] = ga[ch] * basis[k];
                 // ga . d(light)/d(n)  (getJLiNo, RendererUtil.h:371-391)
                 float wt[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -253,6 +250,11 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                 rr[0] = wv[0] * N0.x + wv[1] * N0.y + wv[2] * N0.z;
                 rr[1] = wv[0] * N1.x + wv[1] * N1.y + wv[2] * N1.z;
                 rr[2] = wv[0] * N2.x + wv[1] * N2.y + wv[2] * N2.z;
+                // the SH terms last: their 27 registers are live only up to the reduce-scatter
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) shv[9 * ch + k] = ga[ch] * basis[k];
             }
             if (ALBPOS) {  // + sum_ch G light colour_j
                 const float *Cb = io.colors + (size_t)b * N * 3;
@@ -264,6 +266,36 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                     rr[2] += lg * Cb[3 * i2 + ch];
                 }
             }
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) gl[ch] = G[ch] * JCoAl[ch];
+        }
+    }
+
+    // ---- SH partial sums of this tile, warp part: before the position
+    // phase, so that the 32 per-lane terms are freed before the Jacobian
+    __shared__ float red[kTilePix / 32][27];
+    if constexpr (SHADED) {
+        reduce_scatter_step<32>(shv, lane);
+        reduce_scatter_step<16>(shv, lane);
+        reduce_scatter_step<8>(shv, lane);
+        reduce_scatter_step<4>(shv, lane);
+        reduce_scatter_step<2>(shv, lane);
+        if (lane < 27) red[warp][lane] = shv[0];
+    }
+
+    // ---- position phase: the shading term through the barycentrics
+    // (closed-form Jacobian) and the target-image term
+    float val[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) val[k] = 0.0f;
+    if (f >= 0) {
+        {
+            const Camera &cam = sCam;
+            const float4 *FR = ws.faceRec + ((size_t)b * F + f) * kBwdFaceRows;
+            // Pv: per-pixel vector applied with the stored barycentrics (target term);
+            // Qv[j]: shading term already weighted for corner j
+            float Pv[3] = {0.0f, 0.0f, 0.0f};
+            float Qv[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
             if (SHADED || ALBPOS) {
                 const float4 fr2 = FR[2], fr3 = FR[3], fr4 = FR[4];  // vertex positions
                 const float3 V0 = make_float3(fr2.y, fr2.z, fr2.w);
@@ -355,21 +387,9 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
                 for (int a = 0; a < 3; ++a) {
                     if (POS) val[3 * j + a] = bw[j] * Pv[a] + Qv[j][a];
                     if (SHADED) val[NPOS + 3 * j + a] = bw[j] * wv[a];
-                    if (COL) val[NPOS + NGN + 3 * j + a] = bw[j] * (G[a] * JCoAl[a]);
+                    if (COL) val[NPOS + NGN + 3 * j + a] = bw[j] * gl[a];
                 }
         }
-    }
-
-    // ---- SH partial sums of this tile: warp part first, which frees the
-    // 32 per-lane terms before the face reduction needs its registers
-    __shared__ float red[kTilePix / 32][27];
-    if constexpr (SHADED) {
-        reduce_scatter_step<32>(shv, lane);
-        reduce_scatter_step<16>(shv, lane);
-        reduce_scatter_step<8>(shv, lane);
-        reduce_scatter_step<4>(shv, lane);
-        reduce_scatter_step<2>(shv, lane);
-        if (lane < 27) red[warp][lane] = shv[0];
     }
 
     // ---- per-face pre-reduction and accumulation

@@ -209,15 +209,15 @@ class RenderFunction(torch.autograd.Function):
         ctx.h = h
         ctx.backward_flags = backward_flags
         ctx.save_for_backward(vertex_pos, vertex_color, texture, sh_coeff, target_image, extrinsics, intrinsics,
-                              face, vnorm)
+                              face, bary, vnorm)
         ctx.mark_non_differentiable(face, bary, vnorm, nmap)
         return bary, face, img, vnorm, tout, nmap
 
     @staticmethod
     def backward(ctx, g_bary, g_face, g_render, g_vnorm, g_target, g_nmap):
-        vp, vc, tex, sh, tgt, ex, ix, face, vnorm = ctx.saved_tensors
+        vp, vc, tex, sh, tgt, ex, ix, face, bary, vnorm = ctx.saved_tensors
         h = ctx.h
-        gp, gc, gt, gs = render_backward(h, g_render, vp, vc, tex, sh, tgt, vnorm, None, face, g_target, ex, ix,
+        gp, gc, gt, gs = render_backward(h, g_render, vp, vc, tex, sh, tgt, vnorm, bary, face, g_target, ex, ix,
                                          ctx.backward_flags)
         return None, gp, gc, gt, gs, None, None, None, None
 

@@ -127,7 +127,7 @@ typedef struct {
     const float *sh_coeff;        /* [B,C,27]                                   */
     const float *target_image;    /* [B,C,H,W,3]; may be NULL if target_grad is NULL */
     const float *vertex_normal;   /* [B,C,N,3] (forward output)                 */
-    const float *barycentric;     /* [B,C,H,W,2] accepted; barycentrics are recomputed from `face` */
+    const float *barycentric;     /* [B,C,H,W,2] (forward output); NULL = recomputed from `face` */
     const int32_t *face;          /* [B,C,H,W] (forward output)                 */
     const float *target_grad;     /* [B,C,H,W,3] upstream grad of target_image_out, or NULL = 0 */
     const float *extrinsics;      /* [B,C,12]                                   */

@@ -15,7 +15,8 @@ def test_algorithmic_bytes_of_the_bench_workload():
     assert step == P * 64 + C * (12 * N + 12 * F + 24 * F + 12 * N) + 24 * Ht * Wt + 24 * N + 216 * C
     assert step == 589_758_896
     assert bench.kernel_bytes("k_raster", P, C, N, F, Ht, Wt, 1, 0) == 237_429_696
-    assert bench.kernel_bytes("k_bwd_pixels", P, C, N, F, Ht, Wt, 1, 0) == P * 16 + C * (12 * N + 36 * F) + 24 * Ht * Wt
+    # upstream gradient 12 + face id 4 + barycentrics 8 per pixel
+    assert bench.kernel_bytes("k_bwd_pixels", P, C, N, F, Ht, Wt, 1, 0) == P * 24 + C * (12 * N + 36 * F) + 24 * Ht * Wt
     assert bench.kernel_bytes("k_cameras", P, C, N, F, Ht, Wt, 1, 0) is None
 
 

@@ -208,3 +208,42 @@ def test_forward_is_deterministic_and_workspace_paths_agree():
     small = torch.empty(h.forward_workspace_size(1) - 256, dtype=torch.uint8, device=_dev())
     args.workspace, args.workspace_bytes = ctypes.c_void_p(small.data_ptr()), small.numel()
     assert h._L.gvr_forward(h.ptr, ctypes.byref(args), None) == -4
+
+
+@pytest.mark.parametrize("albedo", ["textured", "vertexColor"])
+def test_backward_reads_the_barycentric_input(albedo):
+    """The backward takes the barycentrics from its input, as the reference's
+    grad does (CUDABasedRasterizationGrad.cu:210-211): given perturbed
+    barycentrics it follows the oracle given the same ones.  Without the
+    input it recomputes them from the face ids and equals the call given the
+    forward's own (float atomics only reorder sums)."""
+    import torch
+    from gvr import renderer
+    s = small_scene(num_faces=1280, views=2, size=64, albedo=albedo, shading="shaded", tex=16, seed=31)
+    h = _handle(s)
+    t = _tensors(s)
+    bary, face, img, vn, _, _ = renderer.render_forward(h, t["vertex_pos"], t["vertex_color"], t["texture"],
+                                                        t["sh_coeff"], t["extrinsics"], t["intrinsics"])
+    rng = np.random.default_rng(31)
+    noise = torch.from_numpy(rng.uniform(-0.02, 0.02, tuple(bary.shape)).astype(np.float32)).to(_dev())
+    pert = (bary + noise * (face >= 0).unsqueeze(-1)).contiguous()
+
+    def grads(b):
+        g = renderer.render_backward(h, t["grad_render"], t["vertex_pos"], t["vertex_color"], t["texture"],
+                                     t["sh_coeff"], t["target_image"], vn, b, face, None, t["extrinsics"],
+                                     t["intrinsics"])
+        torch.cuda.synchronize()
+        return [x.cpu().numpy()[0] for x in g]
+
+    keys = ("vertex_pos_grad", "vertex_color_grad", "texture_grad", "sh_coeff_grad")
+    rays = h.debug_rays(t["extrinsics"], t["intrinsics"]).cpu().numpy()[0]
+    o = oracle_scene(s, 0, rays=rays)
+    g_orc = o.backward(face.cpu().numpy()[0], pert.cpu().numpy()[0], vn.cpu().numpy()[0], s["grad_render"][0],
+                       s["target_image"][0], np.zeros_like(s["grad_target"][0]))
+    for k, x in zip(keys, grads(pert)):
+        if np.all(g_orc[k] == 0):
+            assert np.all(x == 0), k
+        else:
+            assert rel_norm(x, g_orc[k]) <= GRAD_TOL, (k, rel_norm(x, g_orc[k]))
+    for k, x, y in zip(keys, grads(None), grads(bary)):
+        assert rel_norm(x, y) <= 1e-6 if np.any(y) else np.all(x == 0), k
