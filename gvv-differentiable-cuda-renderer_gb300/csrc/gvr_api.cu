@@ -21,8 +21,9 @@ struct GvrHandle {
     float *d_uvs;
     int32_t *d_vstart;
     int32_t *d_vfaces;
+    int4 *d_vcsr;
 
-    gvr::Topology topo() const { return gvr::Topology{d_faces, d_uvs, d_vstart, d_vfaces, N, F}; }
+    gvr::Topology topo() const { return gvr::Topology{d_faces, d_uvs, d_vstart, d_vfaces, d_vcsr, N, F}; }
 };
 
 namespace {
@@ -228,6 +229,11 @@ int gvr_create(const GvrTopology *topo, const GvrAttrs *attrs, GvrHandle **out) 
         if (b != a) adj[start[b] + fill[b]++] = f;
         if (c != a && c != b) adj[start[c] + fill[c]++] = f;
     }
+    std::vector<int4> csr(adj.size());
+    for (int k = 0; k < nnz; ++k) {
+        const int f = adj[k];
+        csr[k] = make_int4(topo->faces[3 * f], topo->faces[3 * f + 1], topo->faces[3 * f + 2], f);
+    }
 
     GvrHandle *h = new GvrHandle();
     std::memset(h, 0, sizeof(*h));
@@ -250,6 +256,7 @@ int gvr_create(const GvrTopology *topo, const GvrAttrs *attrs, GvrHandle **out) 
         {(void **)&h->d_uvs, uvs.data(), uvs.size() * sizeof(float)},
         {(void **)&h->d_vstart, start.data(), start.size() * sizeof(int32_t)},
         {(void **)&h->d_vfaces, adj.data(), adj.size() * sizeof(int32_t)},
+        {(void **)&h->d_vcsr, csr.data(), csr.size() * sizeof(int4)},
     };
     for (auto &u : ups) {
         if ((e = cudaMalloc(u.dst, u.bytes)) != cudaSuccess || (e = cudaMemcpy(*u.dst, u.src, u.bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
@@ -268,6 +275,7 @@ void gvr_destroy(GvrHandle *h) {
     cudaFree(h->d_uvs);
     cudaFree(h->d_vstart);
     cudaFree(h->d_vfaces);
+    cudaFree(h->d_vcsr);
     delete h;
 }
 

@@ -430,7 +430,7 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
             float s = 0.0f;
 #pragma unroll
             for (int w = 0; w < kTilePix / 32; ++w) s += red[w][tid];
-            ws.shPartial[((size_t)bc * T + tile) * 27 + tid] = s;
+            ws.shPartial[((size_t)bc * 27 + tid) * T + tile] = s;  // coefficient-major: the finalize reads rows
         }
     }
 }
@@ -470,52 +470,82 @@ __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels_batched(const BwdJob
 
 // ---------------------------------------------------------------------------- vertex gathers
 
+// LANES consecutive threads share vertex i (sub = 0 .. LANES-1): thread sub
+// takes faces sub, sub + LANES, ... of the vertex and the group adds its
+// partial sums by a fixed butterfly (the same bits in every lane, whatever
+// the schedule).  A vertex's few faces leave one thread per vertex with too
+// little independent work to hide the gathers' latency.  All LANES threads
+// of a group must reach the butterfly; `valid` is false past the last vertex.
+template <int LANES, int NV>
+__device__ __forceinline__ void lane_group_sum(float (&x)[NV]) {
+#pragma unroll
+    for (int o = 1; o < LANES; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) x[k] += __shfl_xor_sync(0xffffffffu, x[k], o);
+}
+
+constexpr int kGatherLanes = 4;
+
 // Face-accumulator layout (floats): [0..8] position grad of corners 0..2,
 // [9..17] vertex-normal grad of corners 0..2, [20..28] colour grad of corners 0..2.
+template <int LANES>
 __device__ __forceinline__ void gather_a_item(const Topology &topo, const float *__restrict__ faceAcc,
                                               float *__restrict__ vpos_grad, float *__restrict__ vcol_grad,
-                                              float4 *__restrict__ gN, int useCol, int useGN, int i) {
+                                              float4 *__restrict__ gN, int useCol, int useGN, int i, int sub,
+                                              bool valid) {
     const int N = topo.N, F = topo.F;
-    int b = i / N, v = i - b * N;
-    float pos[3] = {0, 0, 0}, gn[3] = {0, 0, 0}, col[3] = {0, 0, 0};
-    for (int k = topo.vstart[v]; k < topo.vstart[v + 1]; ++k) {
-        int f = topo.vfaces[k];
-        const float *A = faceAcc + ((size_t)b * F + f) * kFaceAccFloats;
+    const int b = i / N, v = i - b * N;
+    float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // position, normal and colour grads
+    const float *Ab = faceAcc + (size_t)b * F * kFaceAccFloats;
+    // the face's vertex ids and its id in one 16-byte load; the corners at v
+    // follow from the ids, so the accumulator loads depend on one load only
+    const int k0 = valid ? topo.vstart[v] + sub : 0, k1 = valid ? topo.vstart[v + 1] : 0;
+    for (int k = k0; k < k1; k += LANES) {
+        const int4 q = topo.vcsr[k];
+        const float *A = Ab + (size_t)q.w * kFaceAccFloats;
+        const int ids[3] = {q.x, q.y, q.z};
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-            if (topo.faces[3 * f + r] != v) continue;
+            if (ids[r] != v) continue;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                pos[a] += A[3 * r + a];
-                gn[a] += A[9 + 3 * r + a];
-                col[a] += A[20 + 3 * r + a];
+                acc[a] += A[3 * r + a];
+                acc[3 + a] += A[9 + 3 * r + a];
+                acc[6 + a] += A[20 + 3 * r + a];
             }
         }
     }
+    if (LANES > 1) lane_group_sum<LANES>(acc);
+    if (!valid || sub != 0) return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        vpos_grad[3 * (size_t)i + a] = pos[a];
-        vcol_grad[3 * (size_t)i + a] = useCol ? col[a] : 0.0f;
+        vpos_grad[3 * (size_t)i + a] = acc[a];
+        vcol_grad[3 * (size_t)i + a] = useCol ? acc[6 + a] : 0.0f;
     }
-    if (useGN) gN[i] = make_float4(gn[0], gn[1], gn[2], 0.0f);
+    if (useGN) gN[i] = make_float4(acc[3], acc[4], acc[5], 0.0f);
 }
 
+// kGatherLanes threads per vertex (the grid covers B*N*kGatherLanes threads).
 __global__ void k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc, float *__restrict__ vpos_grad,
                            float *__restrict__ vcol_grad, float4 *__restrict__ gN, int useCol, int useGN) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < B * topo.N) gather_a_item(topo, faceAcc, vpos_grad, vcol_grad, gN, useCol, useGN, i);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t / kGatherLanes), sub = (int)(t % kGatherLanes);
+    gather_a_item<kGatherLanes>(topo, faceAcc, vpos_grad, vcol_grad, gN, useCol, useGN, i, sub, i < B * topo.N);
 }
 
+template <int LANES>
 __device__ __forceinline__ void gather_b_item(const Topology &topo, const float *__restrict__ verts,
-                                              const float4 *__restrict__ gN, float *__restrict__ vpos_grad, int i) {
+                                              const float4 *__restrict__ gN, float *__restrict__ vpos_grad, int i,
+                                              int sub, bool valid) {
     const int N = topo.N;
-    int b = i / N, v = i - b * N;
+    const int b = i / N, v = i - b * N;
     const float *V = verts + (size_t)b * N * 3;
     const float4 *g = gN + (size_t)b * N;
     float acc[3] = {0, 0, 0};
-    for (int k = topo.vstart[v]; k < topo.vstart[v + 1]; ++k) {
-        int f = topo.vfaces[k];
-        int a[3] = {topo.faces[3 * f], topo.faces[3 * f + 1], topo.faces[3 * f + 2]};
+    const int k0 = valid ? topo.vstart[v] + sub : 0, k1 = valid ? topo.vstart[v + 1] : 0;
+    for (int k = k0; k < k1; k += LANES) {
+        const int4 q = topo.vcsr[k];  // the face's vertex ids
+        const int a[3] = {q.x, q.y, q.z};
         float4 s = g[a[0]];
         if (a[1] != a[0]) { float4 t = g[a[1]]; s.x += t.x; s.y += t.y; s.z += t.z; }
         if (a[2] != a[0] && a[2] != a[1]) { float4 t = g[a[2]]; s.x += t.x; s.y += t.y; s.z += t.z; }
@@ -529,14 +559,18 @@ __device__ __forceinline__ void gather_b_item(const Topology &topo, const float 
             acc[2] += e[0] * s.y - e[1] * s.x;
         }
     }
+    if (LANES > 1) lane_group_sum<LANES>(acc);
+    if (!valid || sub != 0) return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) vpos_grad[3 * (size_t)i + a] += acc[a];
 }
 
+// kGatherLanes threads per vertex.
 __global__ void k_gather_b(const Topology topo, int B, const float *__restrict__ verts, const float4 *__restrict__ gN,
                            float *__restrict__ vpos_grad) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < B * topo.N) gather_b_item(topo, verts, gN, vpos_grad, i);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t / kGatherLanes), sub = (int)(t % kGatherLanes);
+    gather_b_item<kGatherLanes>(topo, verts, gN, vpos_grad, i, sub, i < B * topo.N);
 }
 
 // Both gathers over every job of a batched plan (WHICH 0: gather_a, 1: gather_b).
@@ -548,34 +582,39 @@ __global__ void __launch_bounds__(256) k_gather_batched(const BwdJob *__restrict
     const int i = (blockIdx.x - blockStart[j]) * 256 + threadIdx.x;
     if (J.zeroMode || i >= J.dims.B * J.topo.N) return;
     if (WHICH == 0)
-        gather_a_item(J.topo, reinterpret_cast<const float *>(J.ws.faceAcc), J.vpos_grad, J.vcol_grad, J.ws.gN,
-                      J.useCol, J.shaded, i);
+        gather_a_item<1>(J.topo, reinterpret_cast<const float *>(J.ws.faceAcc), J.vpos_grad, J.vcol_grad, J.ws.gN,
+                         J.useCol, J.shaded, i, 0, true);
     else if (J.shaded)
-        gather_b_item(J.topo, J.io.verts, J.ws.gN, J.vpos_grad, i);
+        gather_b_item<1>(J.topo, J.io.verts, J.ws.gN, J.vpos_grad, i, 0, true);
 }
 
-// One block per (batch, view, coefficient): thread i sums tiles i, i+256, ...
-// (FP32 with compensation), then a fixed-order FP64 tree finishes, so the
-// result is deterministic and FP64-accurate at FP32 cost.
+// One block per (batch, view, coefficient), reading that coefficient's row
+// of tile partials: thread i sums tiles i, i+256, ... (FP32 with
+// compensation), then a fixed-order FP64 reduction (warp shuffles, then the
+// eight warp sums in order) finishes, so the result is deterministic and
+// FP64-accurate at FP32 cost.
 __device__ __forceinline__ void sh_finalize_block(const float *__restrict__ partial, float *__restrict__ sh_grad,
                                                   int tilesPerView, int shaded, int blk) {
-    __shared__ double red[256];
+    __shared__ double red[8];
     const int bc = blk / 27, k = blk % 27;
     float s = 0.0f, comp = 0.0f;
     if (shaded)
         for (int t = threadIdx.x; t < tilesPerView; t += 256) {
             float hi, lo;
-            two_sum(s, partial[((size_t)bc * tilesPerView + t) * 27 + k], hi, lo);
+            two_sum(s, partial[((size_t)bc * 27 + k) * tilesPerView + t], hi, lo);
             s = hi;
             comp += lo;
         }
-    red[threadIdx.x] = (double)s + (double)comp;
+    double d = (double)s + (double)comp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += red[w];
+        sh_grad[(size_t)bc * 27 + k] = (float)t;
     }
-    if (threadIdx.x == 0) sh_grad[(size_t)bc * 27 + k] = (float)red[0];
 }
 
 __global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
@@ -726,13 +765,14 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     CallPixels call{topo, dims, ws, io, st};
     if ((err = visit_variant(dims.albedo, shaded, target, albpos, call))) return err;
     GVR_LAUNCH(st, "k_gather_a",
-               k_gather_a<<<blocks((size_t)B * N, 256), 256, 0, st>>>(
+               k_gather_a<<<blocks((size_t)B * N * kGatherLanes, 256), 256, 0, st>>>(
                    topo, B, reinterpret_cast<const float *>(ws.faceAcc), a.vertex_pos_grad, a.vertex_color_grad, ws.gN,
                    dims.albedo == GVR_ALBEDO_VERTEX_COLOR, shaded));
     if ((err = cudaGetLastError())) return err;
     if (shaded) {
         GVR_LAUNCH(st, "k_gather_b",
-                   k_gather_b<<<blocks((size_t)B * N, 256), 256, 0, st>>>(topo, B, a.vertex_pos, ws.gN, a.vertex_pos_grad));
+                   k_gather_b<<<blocks((size_t)B * N * kGatherLanes, 256), 256, 0, st>>>(topo, B, a.vertex_pos, ws.gN,
+                                                                                        a.vertex_pos_grad));
         if ((err = cudaGetLastError())) return err;
     }
     GVR_LAUNCH(st, "k_sh_finalize", k_sh_finalize<<<B * C * 27, 256, 0, st>>>(ws.shPartial, a.sh_coeff_grad, T, shaded));

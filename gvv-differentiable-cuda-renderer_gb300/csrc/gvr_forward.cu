@@ -9,7 +9,7 @@
 //   k_vertices    vertex normals (:148-174) + projection (:98-115) B*N threads
 //   k_bin_count   face boxes (:184-208), screen-space skip-test
 //                 constants, per-tile counts                     B*C*F threads
-//   k_scan_tiles  exclusive scan of the tile counts              1 block
+//   k_scan_tiles  exclusive scan of the tile counts              8192 per block
 //   k_bin_fill    per-tile face lists                            B*C*F threads
 //   k_raster      one tile per block (replaces :215-408)
 //
@@ -166,7 +166,10 @@ __device__ __forceinline__ void face_geo_item(const float *__restrict__ verts, c
 
 // ---------------------------------------------------------------------------- vertex stage
 
-__device__ __forceinline__ void vertex_item(const FwdJob &J, int i) {
+// Vertex i for views sub, sub + lanes, ...: `lanes` threads share a vertex,
+// each summing its normal (in the same order, so to the same bits; their
+// loads are the same addresses) and projecting it into its share of views.
+__device__ __forceinline__ void vertex_item(const FwdJob &J, int i, int sub = 0, int lanes = 1) {
     const Topology &topo = J.topo;
     const int N = topo.N, F = topo.F, C = J.dims.C;
     int b = i / N, v = i - b * N;
@@ -179,7 +182,7 @@ __device__ __forceinline__ void vertex_item(const FwdJob &J, int i) {
         else acc = v3(xa(acc.x, n.x), xa(acc.y, n.y), xa(acc.z, n.z));
     }
     V3 p = ld3(J.io.verts + (size_t)i * 3);
-    for (int c = 0; c < C; ++c) {
+    for (int c = sub; c < C; c += lanes) {
         size_t o = ((size_t)b * C + c) * N + v;
         float *dst = J.vnormal_out + o * 3;
         dst[0] = acc.x;
@@ -434,9 +437,11 @@ __global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__res
     if (i < B * F) face_geo_item(verts, faces, geo, fnormal, N, F, i, rec, uvs);
 }
 
-__global__ void k_vertices(const FwdJob J) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < J.dims.B * J.topo.N) vertex_item(J, i);
+// `lanes` threads per vertex, each projecting into every lanes-th view.
+__global__ void k_vertices(const FwdJob J, int lanes) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t / lanes), sub = (int)(t % lanes);
+    if (i < J.dims.B * J.topo.N) vertex_item(J, i, sub, lanes);
 }
 
 __global__ void k_bin_count(const FwdJob J) {
@@ -444,8 +449,81 @@ __global__ void k_bin_count(const FwdJob J) {
     if (i < J.dims.B * J.dims.C * J.topo.F) bin_count_item(J, i);
 }
 
+// The same scan by ceil(n / 8192) blocks of 1024 threads, none waiting on
+// another: block j scans counts [8192 j, 8192 (j + 1)) as one pass of
+// scan_block and offsets them by the sum of every count before them, which
+// it adds up itself (at most a few 16-byte loads per thread, L2 hits).
 __global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ count, int *__restrict__ start, int n) {
-    scan_block(count, start, n);
+    __shared__ int warpSum[32];
+    __shared__ int offset;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int base = blockIdx.x * 8192;
+    const bool vec = ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(start)) & 15) == 0;
+    int before = 0;
+    if (vec) {
+        for (int k = 4 * tid; k < base; k += 4096) {  // base is a multiple of 4096
+            const int4 q = *reinterpret_cast<const int4 *>(count + k);
+            before += q.x + q.y + q.z + q.w;
+        }
+    } else {
+        for (int k = tid; k < base; k += 1024) before += count[k];
+    }
+    before = __reduce_add_sync(0xffffffffu, before);
+    if (lane == 0) warpSum[warp] = before;
+    __syncthreads();
+    if (warp == 0) {
+        const int t = __reduce_add_sync(0xffffffffu, warpSum[lane]);
+        if (lane == 0) offset = t;
+    }
+    __syncthreads();
+    const int i0 = base + 8 * tid;
+    int x[8];
+    if (vec && i0 + 8 <= n) {
+        const int4 a = *reinterpret_cast<const int4 *>(count + i0), c = *reinterpret_cast<const int4 *>(count + i0 + 4);
+        x[0] = a.x, x[1] = a.y, x[2] = a.z, x[3] = a.w, x[4] = c.x, x[5] = c.y, x[6] = c.z, x[7] = c.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = i0 + k < n ? count[i0 + k] : 0;
+    }
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sum += x[k];
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    __syncthreads();  // every warp has read warpSum above
+    if (lane == 31) warpSum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int w = warpSum[lane];
+        int wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        warpSum[lane] = wi - w;  // exclusive prefix of warp sums
+    }
+    __syncthreads();
+    int run = offset + warpSum[warp] + incl - sum;
+    int st[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        st[k] = run;
+        run += x[k];
+    }
+    if (vec && i0 + 8 <= n) {
+        *reinterpret_cast<int4 *>(start + i0) = make_int4(st[0], st[1], st[2], st[3]);
+        *reinterpret_cast<int4 *>(start + i0 + 4) = make_int4(st[4], st[5], st[6], st[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (i0 + k < n) start[i0 + k] = st[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && tid == 1023) start[n] = run;  // the last thread's run is the total
 }
 
 __global__ void k_bin_fill(const FwdJob J) {
@@ -562,7 +640,9 @@ cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *g
 }
 
 static cudaError_t launch_vertices(const FwdJob &J, cudaStream_t st) {
-    GVR_LAUNCH(st, "k_vertices", k_vertices<<<blocks((size_t)J.dims.B * J.topo.N, 256), 256, 0, st>>>(J));
+    const int lanes = J.dims.C >= 4 ? 4 : J.dims.C;  // threads per vertex: the views split over them
+    GVR_LAUNCH(st, "k_vertices",
+               k_vertices<<<blocks((size_t)J.dims.B * J.topo.N * lanes, 256), 256, 0, st>>>(J, lanes));
     return cudaGetLastError();
 }
 
@@ -591,7 +671,8 @@ cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
     const size_t nvf = (size_t)B * C * J.topo.F;
     GVR_LAUNCH(st, "k_bin_count", k_bin_count<<<blocks(nvf, 256), 256, 0, st>>>(J));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    GVR_LAUNCH(st, "k_scan_tiles", k_scan_tiles<<<1, 1024, 0, st>>>(J.ws.tileCount, J.ws.tileStart, B * C * T));
+    const int nt = B * C * T;
+    GVR_LAUNCH(st, "k_scan_tiles", k_scan_tiles<<<(nt + 8191) / 8192, 1024, 0, st>>>(J.ws.tileCount, J.ws.tileStart, nt));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     GVR_LAUNCH(st, "k_bin_fill", k_bin_fill<<<blocks(nvf, 256), 256, 0, st>>>(J));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;

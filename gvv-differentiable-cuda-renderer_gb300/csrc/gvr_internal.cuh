@@ -303,7 +303,9 @@ struct Topology {
     const int32_t *faces;   // [F*3]
     const float *uvs;       // [F*6]
     const int32_t *vstart;  // [N+1]
-    const int32_t *vfaces;  // [nnz]
+    const int32_t *vfaces;  // [nnz] faces around each vertex, ascending
+    const int4 *vcsr;       // [nnz] the same faces as (i0, i1, i2, f): a gather reads the face's
+                            // vertex ids (and so its corners at the vertex) with its id in one load
     int N, F;
 };
 
@@ -385,7 +387,7 @@ struct BwdScratch {
     float4 *faceRec;     // [B*F*kBwdFaceRows]
     float4 *faceAcc;     // [B*F*kFaceAccFloats/4]
     float4 *gN;          // [B*N] normal-gradient accumulator per vertex
-    float *shPartial;    // [B*C*T*27]
+    float *shPartial;    // [B*C][27][T] per-tile SH partial sums
 };
 
 // Inputs and outputs of the backward's pixel kernel.
