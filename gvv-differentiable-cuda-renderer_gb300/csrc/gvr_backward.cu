@@ -440,6 +440,7 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
 template <int MODE, bool SHADED, bool TARGET, bool ALBPOS = false>
 __global__ void __launch_bounds__(kTilePix, 4) k_bwd_pixels(const Topology topo, const FrameDims dims, const BwdScratch ws,
                                                          const BwdIO io, int bcBase) {
+    pdl_enter();
     bwd_tile<MODE, SHADED, TARGET, ALBPOS>(topo, dims, ws, io, bcBase + blockIdx.z, blockIdx.x, blockIdx.y);
 }
 
@@ -528,6 +529,7 @@ __device__ __forceinline__ void gather_a_item(const Topology &topo, const float 
 // kGatherLanes threads per vertex (the grid covers B*N*kGatherLanes threads).
 __global__ void k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc, float *__restrict__ vpos_grad,
                            float *__restrict__ vcol_grad, float4 *__restrict__ gN, int useCol, int useGN) {
+    pdl_enter();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t / kGatherLanes), sub = (int)(t % kGatherLanes);
     gather_a_item<kGatherLanes>(topo, faceAcc, vpos_grad, vcol_grad, gN, useCol, useGN, i, sub, i < B * topo.N);
@@ -568,6 +570,7 @@ __device__ __forceinline__ void gather_b_item(const Topology &topo, const float 
 // kGatherLanes threads per vertex.
 __global__ void k_gather_b(const Topology topo, int B, const float *__restrict__ verts, const float4 *__restrict__ gN,
                            float *__restrict__ vpos_grad) {
+    pdl_enter();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t / kGatherLanes), sub = (int)(t % kGatherLanes);
     gather_b_item<kGatherLanes>(topo, verts, gN, vpos_grad, i, sub, i < B * topo.N);
@@ -619,6 +622,7 @@ __device__ __forceinline__ void sh_finalize_block(const float *__restrict__ part
 
 __global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
                                                      int tilesPerView, int shaded) {
+    pdl_enter();
     sh_finalize_block(partial, sh_grad, tilesPerView, shaded, blockIdx.x);
 }
 
@@ -705,9 +709,10 @@ struct CallPixels {
         const int BC = dims.B * dims.C;
         for (int bc0 = 0; bc0 < BC; bc0 += 65535) {  // gridDim.z holds at most 65535 views
             const dim3 grid(dims.tilesX, dims.tilesY, min(65535, BC - bc0));
+            cudaError_t e;
             GVR_LAUNCH(st, "k_bwd_pixels",
-                       (k_bwd_pixels<MODE, SHADED, TARGET, ALBPOS><<<grid, kTilePix, 0, st>>>(topo, dims, ws, io, bc0)));
-            const cudaError_t e = cudaGetLastError();
+                       e = launch_pdl(k_bwd_pixels<MODE, SHADED, TARGET, ALBPOS>, grid, dim3(kTilePix), 0, st, topo, dims,
+                                      ws, io, bc0));
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
@@ -764,19 +769,23 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     const bool albpos = (a.flags & GVR_BACKWARD_ALBEDO_POSITION) != 0;
     CallPixels call{topo, dims, ws, io, st};
     if ((err = visit_variant(dims.albedo, shaded, target, albpos, call))) return err;
+    const int useCol = dims.albedo == GVR_ALBEDO_VERTEX_COLOR, useGN = shaded;
     GVR_LAUNCH(st, "k_gather_a",
-               k_gather_a<<<blocks((size_t)B * N * kGatherLanes, 256), 256, 0, st>>>(
-                   topo, B, reinterpret_cast<const float *>(ws.faceAcc), a.vertex_pos_grad, a.vertex_color_grad, ws.gN,
-                   dims.albedo == GVR_ALBEDO_VERTEX_COLOR, shaded));
-    if ((err = cudaGetLastError())) return err;
+               err = launch_pdl(k_gather_a, dim3(blocks((size_t)B * N * kGatherLanes, 256)), dim3(256), 0, st, topo, B,
+                                reinterpret_cast<const float *>(ws.faceAcc), a.vertex_pos_grad, a.vertex_color_grad,
+                                ws.gN, useCol, useGN));
+    if (err) return err;
     if (shaded) {
         GVR_LAUNCH(st, "k_gather_b",
-                   k_gather_b<<<blocks((size_t)B * N * kGatherLanes, 256), 256, 0, st>>>(topo, B, a.vertex_pos, ws.gN,
-                                                                                        a.vertex_pos_grad));
-        if ((err = cudaGetLastError())) return err;
+                   err = launch_pdl(k_gather_b, dim3(blocks((size_t)B * N * kGatherLanes, 256)), dim3(256), 0, st,
+                                    topo, B, a.vertex_pos, (const float4 *)ws.gN, a.vertex_pos_grad));
+        if (err) return err;
     }
-    GVR_LAUNCH(st, "k_sh_finalize", k_sh_finalize<<<B * C * 27, 256, 0, st>>>(ws.shPartial, a.sh_coeff_grad, T, shaded));
-    return cudaGetLastError();
+    const int shadedFlag = shaded;
+    GVR_LAUNCH(st, "k_sh_finalize",
+               err = launch_pdl(k_sh_finalize, dim3(B * C * 27), dim3(256), 0, st, (const float *)ws.shPartial,
+                                a.sh_coeff_grad, T, shadedFlag));
+    return err;
 }
 
 // The batched backward of many jobs: one clearing launch, the camera and face

@@ -439,12 +439,14 @@ __global__ void k_face_geo(const float *__restrict__ verts, const int32_t *__res
 
 // `lanes` threads per vertex, each projecting into every lanes-th view.
 __global__ void k_vertices(const FwdJob J, int lanes) {
+    pdl_enter();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t / lanes), sub = (int)(t % lanes);
     if (i < J.dims.B * J.topo.N) vertex_item(J, i, sub, lanes);
 }
 
 __global__ void k_bin_count(const FwdJob J) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < J.dims.B * J.dims.C * J.topo.F) bin_count_item(J, i);
 }
@@ -454,6 +456,7 @@ __global__ void k_bin_count(const FwdJob J) {
 // scan_block and offsets them by the sum of every count before them, which
 // it adds up itself (at most a few 16-byte loads per thread, L2 hits).
 __global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ count, int *__restrict__ start, int n) {
+    pdl_enter();
     __shared__ int warpSum[32];
     __shared__ int offset;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -527,6 +530,7 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ cou
 }
 
 __global__ void k_bin_fill(const FwdJob J) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < J.dims.B * J.dims.C * J.topo.F) bin_fill_item(J, i);
 }
@@ -586,6 +590,7 @@ __global__ void __launch_bounds__(1024) k_scan_tiles_batched(const FwdJob *__res
 // per-call counters, or the backward's texture gradient).  Threads
 // [0, faces) take faces, the next `views` take cameras, the rest clear.
 __global__ void k_setup(const SetupArgs A) {
+    pdl_enter();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nF = (long long)A.B * A.F;
     if (i < nF) {
@@ -622,8 +627,9 @@ cudaError_t launch_setup(SetupArgs a, cudaStream_t st) {
     const long long zt = a.zero ? (a.zeroVec ? (a.zeroWords + 3) / 4 : a.zeroWords) : 0;
     const long long n = (long long)a.B * a.F + a.views + zt;
     if (n == 0) return cudaSuccess;
-    GVR_LAUNCH(st, "k_setup", k_setup<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a));
-    return cudaGetLastError();
+    cudaError_t err;
+    GVR_LAUNCH(st, "k_setup", err = launch_pdl(k_setup, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, a));
+    return err;
 }
 
 cudaError_t launch_cameras(const float *extr, const float *intr, Camera *cams, int count, cudaStream_t st) {
@@ -641,9 +647,11 @@ cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *g
 
 static cudaError_t launch_vertices(const FwdJob &J, cudaStream_t st) {
     const int lanes = J.dims.C >= 4 ? 4 : J.dims.C;  // threads per vertex: the views split over them
+    cudaError_t err;
     GVR_LAUNCH(st, "k_vertices",
-               k_vertices<<<blocks((size_t)J.dims.B * J.topo.N * lanes, 256), 256, 0, st>>>(J, lanes));
-    return cudaGetLastError();
+               err = launch_pdl(k_vertices, dim3(blocks((size_t)J.dims.B * J.topo.N * lanes, 256)), dim3(256), 0, st,
+                                J, lanes));
+    return err;
 }
 
 cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
@@ -669,13 +677,15 @@ cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
     if (err != cudaSuccess) return err;
     if ((err = launch_vertices(J, st)) != cudaSuccess) return err;
     const size_t nvf = (size_t)B * C * J.topo.F;
-    GVR_LAUNCH(st, "k_bin_count", k_bin_count<<<blocks(nvf, 256), 256, 0, st>>>(J));
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_bin_count", err = launch_pdl(k_bin_count, dim3(blocks(nvf, 256)), dim3(256), 0, st, J));
+    if (err != cudaSuccess) return err;
     const int nt = B * C * T;
-    GVR_LAUNCH(st, "k_scan_tiles", k_scan_tiles<<<(nt + 8191) / 8192, 1024, 0, st>>>(J.ws.tileCount, J.ws.tileStart, nt));
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    GVR_LAUNCH(st, "k_bin_fill", k_bin_fill<<<blocks(nvf, 256), 256, 0, st>>>(J));
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_scan_tiles",
+               err = launch_pdl(k_scan_tiles, dim3((nt + 8191) / 8192), dim3(1024), 0, st,
+                                (const int *)J.ws.tileCount, J.ws.tileStart, nt));
+    if (err != cudaSuccess) return err;
+    GVR_LAUNCH(st, "k_bin_fill", err = launch_pdl(k_bin_fill, dim3(blocks(nvf, 256)), dim3(256), 0, st, J));
+    if (err != cudaSuccess) return err;
     return launch_raster(J, st);
 }
 

@@ -286,6 +286,15 @@ __device__ __forceinline__ float dot2(const float (&x)[K], const float (&y)[K]) 
     return __fadd_rn(p, s);
 }
 
+// First statement of a kernel launched by launch_pdl: lets the next kernel
+// on the stream be launched now (its blocks wait in their own pdl_enter),
+// then waits until the previous kernel has completed and its memory writes
+// are visible.  Without a programmatic predecessor both return at once.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // The job owning block `blk` of a batched launch: the last j with blockStart[j] <= blk.
 __device__ __forceinline__ int job_of_block(const int *__restrict__ blockStart, int nJobs, int blk) {
     int lo = 0, hi = nJobs - 1;

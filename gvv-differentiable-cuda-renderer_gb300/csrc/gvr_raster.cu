@@ -505,6 +505,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
 // One block per tile of one call: grid (tilesX, tilesY, views), views
 // bcBase .. bcBase + gridDim.z - 1.
 __global__ void __launch_bounds__(kTilePix, 5) k_raster(const FwdJob J, int bcBase) {
+    pdl_enter();
     raster_tile(J, bcBase + blockIdx.z, blockIdx.x, blockIdx.y);
 }
 
@@ -556,8 +557,8 @@ cudaError_t launch_raster(const FwdJob &J, cudaStream_t st) {
     const int BC = J.dims.B * J.dims.C;
     for (int bc0 = 0; bc0 < BC; bc0 += 65535) {  // gridDim.z holds at most 65535 views
         const dim3 grid(J.dims.tilesX, J.dims.tilesY, min(65535, BC - bc0));
-        GVR_LAUNCH(st, "k_raster", k_raster<<<grid, kTilePix, 0, st>>>(J, bc0));
-        const cudaError_t e = cudaGetLastError();
+        cudaError_t e;
+        GVR_LAUNCH(st, "k_raster", e = launch_pdl(k_raster, grid, dim3(kTilePix), 0, st, J, bc0));
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
