@@ -222,6 +222,34 @@ __device__ __forceinline__ int4 face_box(float4 p0, float4 p1, float4 p2, int W,
     return r;
 }
 
+// Runs of equal keys in consecutive lanes of the converged group `act`:
+// whether this lane heads its run, its rank in the run, the run's length (in
+// the head) and the head's lane.  Faces next to each other in index order
+// are neighbours on the mesh, so the lanes of a warp meet a tile mostly in
+// runs: one atomic per run stands in for one per lane, found with a shuffle
+// and a ballot (a match over the warp keeps the address-divergence unit busy
+// and stalls the binning kernels).
+struct KeyRun {
+    bool head;
+    int rank, len, headLane;
+};
+
+__device__ __forceinline__ KeyRun key_run(unsigned act, long long key, int lane) {
+    const unsigned below = act & ((1u << lane) - 1u);
+    const int prevLane = below ? 31 - __clz(below) : lane;
+    const long long prev = __shfl_sync(act, key, prevLane);
+    KeyRun r;
+    r.head = !below || prev != key;
+    const unsigned heads = __ballot_sync(act, r.head);
+    r.headLane = 31 - __clz(heads & ((2u << lane) - 1u));  // (2u << 31) - 1 = all lanes
+    r.rank = __popc(below & ~((1u << r.headLane) - 1u));
+    const unsigned after = heads & ~((2u << lane) - 1u);
+    const int end = after ? __ffs(after) - 1 : 32;
+    const unsigned upto = end == 32 ? 0xffffffffu : ((1u << end) - 1u);
+    r.len = __popc(act & upto & ~((1u << lane) - 1u));
+    return r;
+}
+
 __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
     const Topology &topo = J.topo;
     const FrameDims &dims = J.dims;
@@ -317,15 +345,15 @@ __device__ __forceinline__ void bin_count_item(const FwdJob &J, int i) {
         ws.bigList[(size_t)bc * F + k] = f;
         return;
     }
-    // One atomic per distinct tile of the warp per round: the lanes of a warp
-    // hold neighbouring faces, which share most of their tiles.
+    // One atomic per run of lanes meeting the same tile in a round: the lanes
+    // of a warp hold neighbouring faces, which share most of their tiles.
     const unsigned act = __activemask();
     const int lane = threadIdx.x & 31, w = tx1 - tx0 + 1;
     const int rounds = __reduce_max_sync(act, nt);
     for (int r = 0; r < rounds; ++r) {
         const long long key = r < nt ? (long long)bc * T + (ty0 + r / w) * dims.tilesX + tx0 + r % w : -1ll;
-        const unsigned peers = __match_any_sync(act, key);
-        if (key >= 0 && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&ws.tileCount[key], __popc(peers));
+        const KeyRun R = key_run(act, key, lane);
+        if (key >= 0 && R.head) atomicAdd(&ws.tileCount[key], R.len);
     }
 }
 
@@ -406,18 +434,17 @@ __device__ __forceinline__ void bin_fill_item(const FwdJob &J, int i) {
     const int w = tx1 - tx0 + 1, nt = w * (ty1 - ty0 + 1);
     if (nt > dims.bigTiles) return;
     const int T = dims.tilesX * dims.tilesY;
-    // as in the count: one atomic per distinct tile of the warp per round,
-    // the group's slots handed out by rank
+    // as in the count: one atomic per run of lanes meeting the same tile in a
+    // round, the run's slots handed out by rank
     const unsigned act = __activemask();
     const int lane = threadIdx.x & 31;
     const int rounds = __reduce_max_sync(act, nt);
     for (int r = 0; r < rounds; ++r) {
         const long long key = r < nt ? (long long)bc * T + (ty0 + r / w) * dims.tilesX + tx0 + r % w : -1ll;
-        const unsigned peers = __match_any_sync(act, key);
-        const int rank = __popc(peers & ((1u << lane) - 1u));
+        const KeyRun R = key_run(act, key, lane);
         int slot = 0;
-        if (key >= 0 && rank == 0) slot = atomicAdd(&ws.tileCursor[key], __popc(peers));
-        slot = __shfl_sync(act, slot, __ffs(peers) - 1) + rank;
+        if (key >= 0 && R.head) slot = atomicAdd(&ws.tileCursor[key], R.len);
+        slot = __shfl_sync(act, slot, R.headLane) + R.rank;
         if (key >= 0) ws.bins[ws.tileStart[key] + slot] = f;
     }
 }
