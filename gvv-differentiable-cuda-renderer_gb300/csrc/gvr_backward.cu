@@ -163,9 +163,8 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
             const V3 N0 = ld3(VN + 3 * i0), N1 = ld3(VN + 3 * i1), N2 = ld3(VN + 3 * i2);
             const V3 un = pixel_normal_un(N0, N1, N2, abc);
             const float len = __fsqrt_rn(xdot(un, un));
-            V3 n = v3(xd(un.x, len), xd(un.y, len), xd(un.z, len));
-            const bool flipped = xdot(n, d) > 0.0f;
-            if (flipped) n = v3(-n.x, -n.y, -n.z);
+            bool flipped;
+            const V3 n = unit_normal(un, len, d, flipped);
             const float *gr = io.grad_render + 3 * p;
             const float G[3] = {gr[0], gr[1], gr[2]};
             const float *sh = sSH;

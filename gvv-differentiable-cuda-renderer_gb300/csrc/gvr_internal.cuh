@@ -192,6 +192,22 @@ __device__ __forceinline__ V3 pixel_normal_un(V3 n0, V3 n1, V3 n2, V3 abc) {
               xa(xa(xm(n0.z, abc.x), xm(n1.z, abc.y)), xm(n2.z, abc.z)));
 }
 
+// Unit pixel normal n = un / len and the reference's flip decision
+// (n . d > 0 with n's components the IEEE quotients un_i / len,
+// CUDABasedRasterization.cu:308-319).  n is formed with one correctly
+// rounded reciprocal and three products, within 1 ulp of the quotients per
+// component, which moves n . d by less than 1e-6; when |n . d| is below
+// that, the decision is taken on the exact quotients, so it is always the
+// reference's.  Returns n, flipped when `flipped`.
+__device__ __forceinline__ V3 unit_normal(V3 un, float len, V3 d, bool &flipped) {
+    const float inv = __frcp_rn(len);
+    const V3 n = v3(__fmul_rn(un.x, inv), __fmul_rn(un.y, inv), __fmul_rn(un.z, inv));
+    float nd = xdot(n, d);
+    if (fabsf(nd) < 1e-6f) nd = xdot(v3(xd(un.x, len), xd(un.y, len), xd(un.z, len)), d);
+    flipped = nd > 0.0f;
+    return flipped ? v3(-n.x, -n.y, -n.z) : n;
+}
+
 // Nearest-texel texture coordinate (CUDABasedRasterization.cu:326-345):
 // returns the clamped (U0, V0) in texels.
 __device__ __forceinline__ float2 texel_coord6(float u0, float v0, float u1, float v1, float u2, float v2, V3 abc,

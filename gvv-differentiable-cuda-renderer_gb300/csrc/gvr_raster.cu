@@ -426,9 +426,8 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
     const float4 r0 = SR[0], r1 = SR[1];
     const V3 d = x.d;
     V3 un = pixel_normal_un(v3(r0.x, r0.y, r0.z), v3(r0.w, r1.x, r1.y), v3(r1.z, r1.w, SR[2].x), abc);
-    float len = __fsqrt_rn(xdot(un, un));
-    V3 n = v3(xd(un.x, len), xd(un.y, len), xd(un.z, len));
-    if (xdot(n, d) > 0.0f) n = v3(-n.x, -n.y, -n.z);
+    bool flippedN;
+    const V3 n = unit_normal(un, __fsqrt_rn(xdot(un, un)), d, flippedN);
     float3 col;
     switch (dims.albedo) {
         case GVR_ALBEDO_TEXTURED: {
