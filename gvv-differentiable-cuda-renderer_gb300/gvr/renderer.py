@@ -208,16 +208,18 @@ class RenderFunction(torch.autograd.Function):
                                                             extrinsics, intrinsics, target_image, copy_target=True)
         ctx.h = h
         ctx.backward_flags = backward_flags
+        # only the face ids are kept for the backward, which recomputes the
+        # barycentrics from them (no per-pixel intermediates kept)
         ctx.save_for_backward(vertex_pos, vertex_color, texture, sh_coeff, target_image, extrinsics, intrinsics,
-                              face, bary, vnorm)
+                              face, vnorm)
         ctx.mark_non_differentiable(face, bary, vnorm, nmap)
         return bary, face, img, vnorm, tout, nmap
 
     @staticmethod
     def backward(ctx, g_bary, g_face, g_render, g_vnorm, g_target, g_nmap):
-        vp, vc, tex, sh, tgt, ex, ix, face, bary, vnorm = ctx.saved_tensors
+        vp, vc, tex, sh, tgt, ex, ix, face, vnorm = ctx.saved_tensors
         h = ctx.h
-        gp, gc, gt, gs = render_backward(h, g_render, vp, vc, tex, sh, tgt, vnorm, bary, face, g_target, ex, ix,
+        gp, gc, gt, gs = render_backward(h, g_render, vp, vc, tex, sh, tgt, vnorm, None, face, g_target, ex, ix,
                                          ctx.backward_flags)
         return None, gp, gc, gt, gs, None, None, None, None
 
