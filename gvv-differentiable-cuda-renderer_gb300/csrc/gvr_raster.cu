@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(kTilePix, 5) k_raster(const FwdJob J, int bcBa
 // Persistent: a grid sized to the resident capacity pulls (job, view, tile)
 // items from one counter until all jobs' tiles are done.  itemStart[j] is the
 // first item of job j (exclusive prefix of its B*C*tiles).
-__global__ void __launch_bounds__(kTilePix, 3) k_raster_persistent(const FwdJob *__restrict__ jobs,
+__global__ void __launch_bounds__(kTilePix, 4) k_raster_persistent(const FwdJob *__restrict__ jobs,
                                                                 const int *__restrict__ itemStart, int nJobs,
                                                                 int *__restrict__ counter) {
     __shared__ int sItem, sJob, sBC, sTX, sTY;
