@@ -20,7 +20,7 @@
 //                texels get atomics.  What a pixel reads about its face
 //                (vertex indices, texture coordinates, vertex positions)
 //                comes from one 80-byte record per face that the face pass
-//                (k_face_geo) writes.
+//                of the backward's set-up launch (k_setup) writes.
 //  k_gather_a    per vertex, over its CSR faces: colour grad, position grad
 //                (direct terms) and the vertex-normal gradient gN[v].
 //  k_gather_b    per vertex: the normal-adjacency term of :559-615.  The

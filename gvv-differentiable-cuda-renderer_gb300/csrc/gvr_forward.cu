@@ -4,9 +4,9 @@
 // Pipeline for all B x C views of one call (reference: the 7-kernel chain
 // of cpp/src/Renderer/CUDABasedRasterization.cu:449-473, launched once per
 // batch element there):
-//   k_cameras     camera inverses (:23-67)                       B*C threads
-//   k_face_geo    scaled face geometry + face normals (:122-141)  B*F threads
-//   k_vertices    vertex normals (:148-174) + projection (:98-115) B*N threads
+//   k_setup       camera inverses (:23-67), scaled face geometry and
+//                 face normals (:122-141), cleared counters    B*F + B*C + clear
+//   k_vertices    vertex normals (:148-174) + projection (:98-115) B*N*min(C,4)
 //   k_bin_count   face boxes (:184-208), screen-space skip-test
 //                 constants, per-tile counts                     B*C*F threads
 //   k_scan_tiles  exclusive scan of the tile counts              8192 per block

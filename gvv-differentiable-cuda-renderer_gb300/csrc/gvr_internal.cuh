@@ -44,7 +44,7 @@ __device__ __forceinline__ V3 ld3(const float *p) { return v3(p[0], p[1], p[2]);
 
 // ---------------------------------------------------------------------------- per-call records
 
-// Per (batch, view) camera record, written by k_cameras.
+// Per (batch, view) camera record, written by the set-up launch (camera_item).
 struct Camera {
     float invE[16];   // inverse extrinsics (cofactor inverse, FP32)
     float invP[16];   // inverse of K*E
