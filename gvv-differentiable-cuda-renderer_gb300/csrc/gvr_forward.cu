@@ -481,7 +481,8 @@ __global__ void k_bin_count(const FwdJob J) {
 // The same scan by ceil(n / 8192) blocks of 1024 threads, none waiting on
 // another: block j scans counts [8192 j, 8192 (j + 1)) as one pass of
 // scan_block and offsets them by the sum of every count before them, which
-// it adds up itself (at most a few 16-byte loads per thread, L2 hits).
+// it adds up itself (a few 16-byte loads per thread, L2 hits, while the
+// blocks are few; the launcher takes k_scan_tiles_one beyond kScanBlocks).
 __global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ count, int *__restrict__ start, int n) {
     pdl_enter();
     __shared__ int warpSum[32];
@@ -554,6 +555,14 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ cou
             if (i0 + k < n) start[i0 + k] = st[k];
     }
     if (blockIdx.x == gridDim.x - 1 && tid == 1023) start[n] = run;  // the last thread's run is the total
+}
+
+// One block for any n (linear work): the scan of calls with more than
+// kScanBlocks * 8192 tiles, where the blocks of k_scan_tiles would each
+// re-add too many counts.
+__global__ void __launch_bounds__(1024) k_scan_tiles_one(const int *__restrict__ count, int *__restrict__ start, int n) {
+    pdl_enter();
+    scan_block(count, start, n);
 }
 
 __global__ void k_bin_fill(const FwdJob J) {
@@ -707,9 +716,15 @@ cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
     GVR_LAUNCH(st, "k_bin_count", err = launch_pdl(k_bin_count, dim3(blocks(nvf, 256)), dim3(256), 0, st, J));
     if (err != cudaSuccess) return err;
     const int nt = B * C * T;
-    GVR_LAUNCH(st, "k_scan_tiles",
-               err = launch_pdl(k_scan_tiles, dim3((nt + 8191) / 8192), dim3(1024), 0, st,
-                                (const int *)J.ws.tileCount, J.ws.tileStart, nt));
+    constexpr int kScanBlocks = 16;  // beyond this many blocks the re-added prefixes outweigh the parallelism
+    if ((nt + 8191) / 8192 <= kScanBlocks)
+        GVR_LAUNCH(st, "k_scan_tiles",
+                   err = launch_pdl(k_scan_tiles, dim3((nt + 8191) / 8192), dim3(1024), 0, st,
+                                    (const int *)J.ws.tileCount, J.ws.tileStart, nt));
+    else
+        GVR_LAUNCH(st, "k_scan_tiles",
+                   err = launch_pdl(k_scan_tiles_one, dim3(1), dim3(1024), 0, st, (const int *)J.ws.tileCount,
+                                    J.ws.tileStart, nt));
     if (err != cudaSuccess) return err;
     GVR_LAUNCH(st, "k_bin_fill", err = launch_pdl(k_bin_fill, dim3(blocks(nvf, 256)), dim3(256), 0, st, J));
     if (err != cudaSuccess) return err;

@@ -176,20 +176,22 @@ def test_multiview_textured_workload():
     check_batch(s, gpu)
 
 
-def test_views_rendered_together_equal_views_rendered_alone():
+@pytest.mark.parametrize("views", [3, 33])
+def test_views_rendered_together_equal_views_rendered_alone(views):
     """Three 1024x1024 views in one call hold 12,288 tiles, which the tile
-    scan splits over two blocks (the second partly filled); each view must
-    come out bit for bit as when rendered alone (4,096 tiles, one block)."""
+    scan splits over two blocks (the second partly filled); 33 views hold
+    135,168 tiles, scanned by the single-block scan.  Each view must come out
+    bit for bit as when rendered alone (4,096 tiles, one block)."""
     import torch
     from gvr import renderer, scenes
-    s = scenes.scene(5120, 3, 1024, 1024, "textured", "shaded", tex_size=64, seed=6)
+    s = scenes.scene(5120, views, 1024, 1024, "textured", "shaded", tex_size=64, seed=6)
     t = _tensors(s)
     h = _handle(s)
     together = renderer.render_forward(h, t["vertex_pos"], t["vertex_color"], t["texture"], t["sh_coeff"],
                                        t["extrinsics"], t["intrinsics"])[:3]
     h1 = renderer.get_handle(s["faces"], s["uvs"], s["num_vertices"], 1, 1024, 1024, "textured", "shaded",
                              device=_dev())
-    for c in range(3):
+    for c in sorted({0, views // 2, views - 1}):
         alone = renderer.render_forward(h1, t["vertex_pos"], t["vertex_color"], t["texture"],
                                         t["sh_coeff"][:, c:c + 1].contiguous(),
                                         t["extrinsics"][:, c:c + 1].contiguous(),
