@@ -568,6 +568,10 @@ def run_batched(args):
     eager_launches = (n1 - n0) / reps  # graph replays add none here
     fwd_graph_ms = timed(lambda: plan.forward(stream=stream, graph=True))
     fwd_per_call_ms = timed(lambda: plan.forward_per_call(stream=stream))
+    # the same jobs with the one persistent raster kernel instead of per-job lanes
+    plan_p = BatchPlan(jobs, autotune=True, persistent=True)
+    fwd_persistent_ms = timed(lambda: plan_p.forward(stream=stream, graph=True))
+    plan_p.close()
     cfgs = {}
     for j in range(len(jobs)):
         cfgs.setdefault("%dx%d/%d" % plan.tile_config(j), 0)
@@ -587,7 +591,8 @@ def run_batched(args):
             "plan_graph_ms": graph_ms, "plan_eager_ms": eager_ms, "per_call_ms": per_call_ms,
             "per_call_mpix_s": P / (per_call_ms / 1e3) / 1e6,
             "forward_only": {"plan_graph_ms": fwd_graph_ms, "per_call_ms": fwd_per_call_ms,
-                             "plan_graph_mpix_s": P / (fwd_graph_ms / 1e3) / 1e6},
+                             "plan_graph_mpix_s": P / (fwd_graph_ms / 1e3) / 1e6,
+                             "persistent_plan_graph_ms": fwd_persistent_ms},
             "launches_per_step": {"plan": eager_launches, "per_call": per_call_launches},
             "autotune_s": tune_s, "tile_configs": cfgs}
     print(json.dumps(line), flush=True)

@@ -535,6 +535,13 @@ struct GvrPlan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     PlanBackward *bwd = nullptr;
+    // per-job rasters on parallel lanes (forked from and joined to the caller's
+    // stream); no lanes with GVR_PLAN_PERSISTENT
+    std::vector<gvr::FwdJob> hostJobs;
+    std::vector<int> order;                 // jobs by decreasing pixel count
+    std::vector<cudaStream_t> lanes;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
 };
 
 namespace {
@@ -651,8 +658,19 @@ size_t plan_carve(const GvrPlan &p, void *base, std::vector<FwdLayout> &lay, Pla
 }
 
 int plan_forward_body(GvrPlan *p, cudaStream_t st) {
-    cudaError_t e = gvr::launch_forward_batched(p->launch, st);
+    cudaError_t e = gvr::launch_forward_batched(p->launch, st, p->lanes.empty());
     if (e != cudaSuccess) return cuda_fail(e, "batched forward launch");
+    if (!p->lanes.empty()) {
+        e = cudaEventRecord(p->fork, st);
+        for (size_t k = 0; k < p->lanes.size() && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(p->lanes[k], p->fork, 0);
+        for (size_t i = 0; i < p->order.size() && e == cudaSuccess; ++i)
+            e = gvr::launch_raster(p->hostJobs[p->order[i]], p->lanes[i % p->lanes.size()]);
+        for (size_t k = 0; k < p->lanes.size() && e == cudaSuccess; ++k) {
+            e = cudaEventRecord(p->joins[k], p->lanes[k]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, p->joins[k], 0);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "per-job raster lanes");
+    }
     for (const GvrJob &job : p->jobs) {
         const int rc = forward_epilogue(job.handle, &job.forward, st);
         if (rc != GVR_OK) return rc;
@@ -767,6 +785,30 @@ int gvr_plan_create(const GvrJob *jobs, int32_t count, int32_t flags, GvrPlan **
     L.rasterGrid = (int)std::min<long long>((long long)sms * gvr::raster_persistent_blocks_per_sm(), totalItems);
     L.zeroBase = static_cast<char *>(p->d_mem) + z0;
     L.zeroBytes = z1 - z0;
+    p->hostJobs = hostJobs;
+    p->order.resize(count);
+    for (int j = 0; j < count; ++j) p->order[j] = j;
+    std::sort(p->order.begin(), p->order.end(), [&](int x, int y) {
+        const auto px = (long long)hostJobs[x].dims.B * hostJobs[x].dims.C * hostJobs[x].dims.W * hostJobs[x].dims.H;
+        const auto py = (long long)hostJobs[y].dims.B * hostJobs[y].dims.C * hostJobs[y].dims.W * hostJobs[y].dims.H;
+        return px > py;
+    });
+    const int nLanes = (flags & GVR_PLAN_PERSISTENT) ? 0 : std::min(GVR_PLAN_LANES, count);
+    if (nLanes > 0) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+    for (int k = 0; k < nLanes && e == cudaSuccess; ++k) {
+        cudaStream_t s = nullptr;
+        cudaEvent_t ev = nullptr;
+        e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) {
+            p->lanes.push_back(s);
+            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) p->joins.push_back(ev);
+    }
+    if (e != cudaSuccess) {
+        gvr_plan_destroy(p);
+        return cuda_fail(e, "plan lanes");
+    }
     *out_plan = p;
     return GVR_OK;
 }
@@ -1031,6 +1073,9 @@ void gvr_plan_destroy(GvrPlan *p) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->d_mem) cudaFree(p->d_mem);
+    for (cudaStream_t s : p->lanes) cudaStreamDestroy(s);
+    for (cudaEvent_t ev : p->joins) cudaEventDestroy(ev);
+    if (p->fork) cudaEventDestroy(p->fork);
     delete p;
 }
 

@@ -747,7 +747,7 @@ cudaError_t launch_forward_normal_map(const FwdJob &J, int *uvOwner, float *norm
 // The batched forward of many jobs: one launch per stage over all jobs, then
 // the persistent raster.  blockStart[s] holds nJobs + 1 block offsets of
 // stage s (kBatchBlock threads per block); itemStart the raster items.
-cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st) {
+cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st, bool raster) {
     cudaError_t err = cudaMemsetAsync(L.zeroBase, 0, L.zeroBytes, st);
     if (err != cudaSuccess) return err;
     GVR_LAUNCH(st, "k_cameras_batched",
@@ -772,6 +772,7 @@ cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st) {
                k_stage_batched<kStageBinFill><<<L.blocks[kStageBinCount], kBatchBlock, 0, st>>>(
                    L.jobs, L.blockStart[kStageBinCount], L.nJobs));
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if (!raster) return cudaSuccess;
     return launch_raster_persistent(L.jobs, L.itemStart, L.nJobs, L.counter, L.rasterGrid, st);
 }
 

@@ -84,7 +84,7 @@ cudaError_t launch_face_geo(const float *verts, const Topology &topo, FaceGeo *g
                             cudaStream_t st, float4 *bwdRec = nullptr);
 cudaError_t launch_forward(const FwdJob &J, cudaStream_t st);
 cudaError_t launch_forward_normal_map(const FwdJob &J, int *uvOwner, float *normal_map, cudaStream_t st);
-cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st);
+cudaError_t launch_forward_batched(const BatchLaunch &L, cudaStream_t st, bool raster = true);
 cudaError_t launch_normal_map(const Topology &topo, const FrameDims &dims, int *owner, const float *vnormal,
                               float *normal_map, int32_t *face, float *bary, float *render, cudaStream_t st);
 cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const BwdScratch &ws, const GvrBackwardArgs &a,

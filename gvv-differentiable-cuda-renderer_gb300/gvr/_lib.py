@@ -54,6 +54,8 @@ class GvrJob(ctypes.Structure):
 
 
 PLAN_AUTOTUNE = 1
+PLAN_PERSISTENT = 2
+PLAN_LANES = 16
 
 
 class GvrKernelTime(ctypes.Structure):

@@ -33,7 +33,7 @@ class BatchPlan:
     device tensors owned by the plan; update them in place (plan.inputs[j])
     between calls.  Outputs live in plan.outputs[j]."""
 
-    def __init__(self, jobs, autotune=False):
+    def __init__(self, jobs, autotune=False, persistent=False):
         if not jobs:
             raise ValueError("a plan needs at least one job")
         self._L = _lib.load()
@@ -68,8 +68,8 @@ class BatchPlan:
         self._jobs = arr
         plan = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(self._L.gvr_plan_create(arr, len(jobs), _lib.PLAN_AUTOTUNE if autotune else 0,
-                                               ctypes.byref(plan)))
+            flags = (_lib.PLAN_AUTOTUNE if autotune else 0) | (_lib.PLAN_PERSISTENT if persistent else 0)
+            _lib.check(self._L.gvr_plan_create(arr, len(jobs), flags, ctypes.byref(plan)))
         self._plan = plan
 
     def forward(self, stream=None, graph=False):

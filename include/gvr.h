@@ -224,10 +224,13 @@ int gvr_image_gaussian3x3(const float *image, float *out, int32_t batch, int32_t
  *
  * A plan binds a list of forward jobs -- each a handle (mesh topology,
  * views, resolution, modes) with one call's device buffers -- once, and
- * renders all of them with one launch per pipeline stage over every job
- * and one persistent raster kernel that pulls (job, view, tile) items from
- * a shared counter, so meshes of very different sizes share the GPU without
- * per-mesh launches.  Every job's outputs are bit-identical to gvr_forward
+ * renders all of them with one launch per pipeline stage over every job,
+ * then the raster: by default each job's raster kernel on one of
+ * GVR_PLAN_LANES streams forked from and joined to the caller's stream
+ * (largest jobs first; under graph capture they become parallel branches),
+ * or, with GVR_PLAN_PERSISTENT, one persistent raster kernel that pulls
+ * (job, view, tile) items from a shared counter.  Meshes of very different
+ * sizes share the GPU either way.  Every job's outputs are bit-identical to gvr_forward
  * on the same buffers.  The plan owns all scratch (allocated at create);
  * gvr_plan_forward allocates nothing and never synchronises the host, and
  * gvr_plan_forward_graph captures it once into a CUDA graph and replays
@@ -249,6 +252,10 @@ typedef struct {
  * first job of the bucket (the choice is cached for the process); without
  * it they use 16x16 and 16. */
 #define GVR_PLAN_AUTOTUNE 1
+/* One persistent raster kernel over every job instead of a raster kernel per
+ * job on parallel lanes (the same outputs; the lanes measured faster). */
+#define GVR_PLAN_PERSISTENT 2
+#define GVR_PLAN_LANES 16
 
 int gvr_plan_create(const GvrJob *jobs, int32_t count, int32_t flags, GvrPlan **out_plan);
 int gvr_plan_forward(GvrPlan *plan, void *stream);

@@ -116,4 +116,5 @@ def test_python_constants_match_the_header():
         assert h[name] == code, name
     assert _lib.BACKWARD_ALBEDO_POSITION == h["GVR_BACKWARD_ALBEDO_POSITION"]
     assert _lib.PLAN_AUTOTUNE == h["GVR_PLAN_AUTOTUNE"]
+    assert _lib.PLAN_PERSISTENT == h["GVR_PLAN_PERSISTENT"] and _lib.PLAN_LANES == h["GVR_PLAN_LANES"]
     assert _lib.NOALLOC_SCRATCH_BYTES == h["GVR_NOALLOC_SCRATCH_BYTES"]

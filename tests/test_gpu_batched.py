@@ -59,26 +59,28 @@ def _check(plan, jobs):
             assert _same(got[k].cpu().numpy(), ref[k]), (j, k)
 
 
+@pytest.mark.parametrize("persistent", [False, True], ids=["lanes", "persistent"])
 @pytest.mark.parametrize("tile_width,big_tiles", [(16, 16), (32, 4), (8, 16), (16, 1)])
-def test_plan_matches_single_calls(tile_width, big_tiles):
+def test_plan_matches_single_calls(tile_width, big_tiles, persistent):
     import torch
     from gvr.batch import BatchPlan
     dev = torch.device("cuda", 0)
     jobs = _plan_jobs(_jobs(), dev, tile_width=tile_width, big_tiles=big_tiles)
-    plan = BatchPlan(jobs)
+    plan = BatchPlan(jobs, persistent=persistent)
     assert all(plan.tile_config(j) == (tile_width, 256 // tile_width, big_tiles) for j in range(len(jobs)))
     plan.forward()
     _check(plan, jobs)
     plan.close()
 
 
-def test_plan_autotune_and_graph_replay():
+@pytest.mark.parametrize("persistent", [False, True], ids=["lanes", "persistent"])
+def test_plan_autotune_and_graph_replay(persistent):
     import torch
     from gvr.batch import BatchPlan
     dev = torch.device("cuda", 0)
     specs = _jobs(seed=11, meshes=5)
     jobs = _plan_jobs(specs, dev)
-    plan = BatchPlan(jobs, autotune=True)
+    plan = BatchPlan(jobs, autotune=True, persistent=persistent)
     for j in range(len(jobs)):
         w, h, b = plan.tile_config(j)
         assert w in (8, 16, 32) and w * h == 256 and b in (4, 16)
