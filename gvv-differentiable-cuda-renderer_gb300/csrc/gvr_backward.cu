@@ -127,11 +127,21 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
         if (tid < kCamWords) reinterpret_cast<float *>(&sCam)[tid] = reinterpret_cast<const float *>(ws.cams + bc)[tid];
         else if (tid < kCamWords + 27) sSH[tid - kCamWords] = io.sh[(size_t)bc * 27 + (tid - kCamWords)];
     }
-    int f = inImage ? io.face[p] : -1;
+    int f = inImage ? __ldcs(io.face + p) : -1;
     if (f >= F) f = -1;  // ids outside [0, F) carry no face
     // the forward's barycentrics, as the reference's grad reads them
-    // (CUDABasedRasterizationGrad.cu:210-211); loaded alongside the face id
-    const float2 bIn = inImage && io.bary_in ? reinterpret_cast<const float2 *>(io.bary_in)[p] : make_float2(0.0f, 0.0f);
+    // (CUDABasedRasterizationGrad.cu:210-211), and the upstream gradient,
+    // loaded alongside the face id; the per-pixel inputs are read once, so
+    // evict-first loads (ld.global.cs) leave the L2 to the face records,
+    // vertex normals and texels that many pixels share
+    const float2 bIn = inImage && io.bary_in ? __ldcs(reinterpret_cast<const float2 *>(io.bary_in) + p)
+                                             : make_float2(0.0f, 0.0f);
+    float G[3] = {0.0f, 0.0f, 0.0f};
+    if (f >= 0) {
+        G[0] = __ldcs(io.grad_render + 3 * p + 0);
+        G[1] = __ldcs(io.grad_render + 3 * p + 1);
+        G[2] = __ldcs(io.grad_render + 3 * p + 2);
+    }
     __syncthreads();
     float shv[SHADED ? 32 : 1];  // 27 SH terms, padded to a warp for the reduce-scatter
 #pragma unroll
@@ -165,8 +175,6 @@ __device__ __forceinline__ void bwd_tile(const Topology &topo, const FrameDims &
             const float len = __fsqrt_rn(xdot(un, un));
             bool flipped;
             const V3 n = unit_normal(un, len, d, flipped);
-            const float *gr = io.grad_render + 3 * p;
-            const float G[3] = {gr[0], gr[1], gr[2]};
             const float *sh = sSH;
             float basis[9];
             sh_basis(n, basis);

@@ -408,18 +408,21 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
         }
     }
 
+    // the outputs are written once and not read again by this launch:
+    // evict-first stores (st.global.cs) leave the L2 to the face records,
+    // shading records and texels that neighbouring tiles read again
     const size_t p = ((size_t)bc * dims.H + v) * dims.W + u;
     if (best == kEmptyKey) {
-        io.face[p] = -1;
-        reinterpret_cast<float2 *>(io.bary)[p] = make_float2(0.0f, 0.0f);
-        io.render[3 * p + 0] = 0.0f;
-        io.render[3 * p + 1] = 1.0f;
-        io.render[3 * p + 2] = 0.0f;
+        __stcs(io.face + p, -1);
+        __stcs(reinterpret_cast<float2 *>(io.bary) + p, make_float2(0.0f, 0.0f));
+        __stcs(io.render + 3 * p + 0, 0.0f);
+        __stcs(io.render + 3 * p + 1, 1.0f);
+        __stcs(io.render + 3 * p + 2, 0.0f);
         return;
     }
     const int f = (int)(unsigned)(best & 0xffffffffull);
-    io.face[p] = f;
-    reinterpret_cast<float2 *>(io.bary)[p] = make_float2(abc.x, abc.y);
+    __stcs(io.face + p, f);
+    __stcs(reinterpret_cast<float2 *>(io.bary) + p, make_float2(abc.x, abc.y));
 
     // shading (CUDABasedRasterization.cu:307-403) from the face's shading record
     const float4 *SR = ws.shadeRec + ((size_t)b * F + f) * kShadeRows;
@@ -494,9 +497,9 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
         }
         col = make_float3(col.x * l0, col.y * l1, col.z * l2);
     }
-    io.render[3 * p + 0] = col.x;
-    io.render[3 * p + 1] = col.y;
-    io.render[3 * p + 2] = col.z;
+    __stcs(io.render + 3 * p + 0, col.x);
+    __stcs(io.render + 3 * p + 1, col.y);
+    __stcs(io.render + 3 * p + 2, col.z);
 }
 
 }  // namespace
