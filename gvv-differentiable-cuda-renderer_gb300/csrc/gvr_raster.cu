@@ -48,6 +48,29 @@ struct __align__(16) Entry {
     float r0, r1, r2, pad;
 };
 
+// The records this kernel reads (screen and face records, shading records,
+// big-face lists, texels) were written by earlier launches and stay
+// unchanged while it runs: they go through the non-coherent read-only path
+// (ld.global.nc), which also left the compiler fewer live registers to
+// spill.  The tile's bin entries, read once, are evict-first loads.
+__device__ __forceinline__ ViewFace ldg_vf(const ViewFace *p) {
+    ViewFace v;
+    v.hdr = __ldg(&p->hdr);
+    v.z = __ldg(&p->z);
+    v.s0 = __ldg(&p->s0);
+    v.s1 = __ldg(&p->s1);
+    return v;
+}
+
+__device__ __forceinline__ FaceSetup ldg_face(const FaceGeo *p) {
+    FaceGeo g;
+    g.a = __ldg(&p->a);
+    g.b = __ldg(&p->b);
+    g.c = __ldg(&p->c);
+    g.d = __ldg(&p->d);
+    return load_face(&g);
+}
+
 __device__ __forceinline__ Entry make_entry(const ViewFace &vf, int f, int tileX0, int tileY0, int tileW, int tileH) {
     Entry E;
     E.x0 = vf.s0.x;
@@ -147,11 +170,11 @@ struct ExactCtx {
 // rejected.  With needDepth = false (a single candidate) the key of an
 // accepted face is just its id: only acceptance matters then.
 __device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f, V3 &abc, bool needDepth) {
-    const FaceSetup fs = load_face(&x.geo[f]);
+    const FaceSetup fs = ldg_face(&x.geo[f]);
     abc = barycentric(fs, x.origS, xdot(x.origS, fs.n), x.d);
     if (!inside(abc)) return kEmptyKey;
     if (!needDepth) return (unsigned long long)(unsigned)f;
-    const float4 z = x.vface[f].z;
+    const float4 z = __ldg(&x.vface[f].z);
     return depth_key(depth_quantised(abc, z.x, z.y, z.z), f);
 }
 
@@ -232,8 +255,8 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
         bool keep = false;
         Entry E;
         if (e < nAll) {
-            const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
-            E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
+            const int f = e < nTile ? __ldcs(ws.bins + s0 + e) : __ldg(bigList + e - nTile);
+            E = make_entry(ldg_vf(VF + f), f, tileX0, tileY0, tileW, tileH);
             keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
         }
         // 0: no usable bound; 1..kBuckets by depth
@@ -426,19 +449,19 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
 
     // shading (CUDABasedRasterization.cu:307-403) from the face's shading record
     const float4 *SR = ws.shadeRec + ((size_t)b * F + f) * kShadeRows;
-    const float4 r0 = SR[0], r1 = SR[1];
+    const float4 r0 = __ldg(SR), r1 = __ldg(SR + 1);
     const V3 d = x.d;
-    V3 un = pixel_normal_un(v3(r0.x, r0.y, r0.z), v3(r0.w, r1.x, r1.y), v3(r1.z, r1.w, SR[2].x), abc);
+    V3 un = pixel_normal_un(v3(r0.x, r0.y, r0.z), v3(r0.w, r1.x, r1.y), v3(r1.z, r1.w, __ldg(&SR[2].x)), abc);
     bool flippedN;
     const V3 n = unit_normal(un, __fsqrt_rn(xdot(un, un)), d, flippedN);
     float3 col;
     switch (dims.albedo) {
         case GVR_ALBEDO_TEXTURED: {
-            const float4 r2 = SR[2], r3 = SR[3];
+            const float4 r2 = __ldg(SR + 2), r3 = __ldg(SR + 3);
             const float2 tc = texel_coord6(r2.y, r2.z, r2.w, r3.x, r3.y, r3.z, abc, dims.Wt, dims.Ht);
             int LU = __float2int_rz(xs(tc.x, 0.5f)), LV = __float2int_rz(xs(tc.y, 0.5f));
             const float *t = io.texture + (((size_t)b * dims.Ht + LV) * dims.Wt + LU) * 3;
-            col = make_float3(t[0], t[1], t[2]);
+            col = make_float3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
             break;
         }
         case GVR_ALBEDO_VERTEX_COLOR: {
