@@ -245,22 +245,24 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
     }
     if (nAll == 0) __syncthreads();  // (otherwise the first chunk's barriers order these stores)
     for (int c0 = 0; c0 < nAll; c0 += kChunk) {
-        // Each thread builds one entry of the chunk and keeps it in registers
-        // until its place in the front-to-back order is known: a counting
-        // sort into kBuckets depth buckets spanning the view's depth bounds
-        // (faces without a bound go first).  sBucketLo[i] is a lower bound of
-        // the depth bound of entry i and of every entry after it, which is
-        // all the early exit needs.
+        // Each thread builds one entry of the chunk, keeps only its face id
+        // and depth bucket while the block counting-sorts the chunk into
+        // kBuckets depth buckets spanning the view's depth bounds (faces
+        // without a bound go first), then builds the entry again from the
+        // record it just loaded (an L1 hit) and stores it in its sorted slot:
+        // holding the 80-byte entry across the sort's barriers cost spills.
+        // sBucketLo[i] is a lower bound of the depth bound of entry i and of
+        // every entry after it, which is all the early exit needs.
         const int e = c0 + tid;
         bool keep = false;
-        Entry E;
+        int fE = -1;
+        int q = 0;  // 0: no usable bound; 1..kBuckets by depth
         if (e < nAll) {
-            const int f = e < nTile ? __ldcs(ws.bins + s0 + e) : __ldg(bigList + e - nTile);
-            E = make_entry(ldg_vf(VF + f), f, tileX0, tileY0, tileW, tileH);
+            fE = e < nTile ? __ldcs(ws.bins + s0 + e) : __ldg(bigList + e - nTile);
+            const Entry E = make_entry(ldg_vf(VF + fE), fE, tileX0, tileY0, tileW, tileH);
             keep = E.bx0 <= E.bx1 && E.by0 <= E.by1 && may_cover_rect(E);
+            q = !keep || !(E.zLowSafe >= lo) ? 0 : 1 + min(kBuckets - 1, (int)((E.zLowSafe - lo) * scale));
         }
-        // 0: no usable bound; 1..kBuckets by depth
-        const int q = !keep || !(E.zLowSafe >= lo) ? 0 : 1 + min(kBuckets - 1, (int)((E.zLowSafe - lo) * scale));
         __syncthreads();  // every warp is done walking the previous chunk; the histogram is clear
         if (keep) atomicAdd(&sHist[q], 1);
         const int nE = __syncthreads_count(keep);
@@ -292,7 +294,7 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
         __syncthreads();
         if (keep) {
             const int pos = atomicAdd(&sHist[q], 1);  // < nE <= kChunk
-            sE[pos] = E;
+            sE[pos] = make_entry(ldg_vf(VF + fE), fE, tileX0, tileY0, tileW, tileH);
             // the bucket's lower edge, pulled down by 0.1% of its offset so rounding
             // in the bucket index can never leave a member below it
             sBucketLo[pos] = q == 0 ? -kInf : q == 1 ? lo : lo + (float)(q - 1) * edge;
