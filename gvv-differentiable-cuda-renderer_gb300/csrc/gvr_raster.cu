@@ -180,7 +180,10 @@ __device__ __forceinline__ unsigned long long exact_key(const ExactCtx &x, int f
 
 // Tile (tx, ty) of view bc (= batch * C + camera) of job J (256 threads, one
 // pixel each).  Shared by the per-call grid kernel and the persistent
-// batched kernel, so both produce the same bits.
+// batched kernel, so both produce the same bits.  ALB >= 0 compiles the
+// shading for that albedo mode only (fewer live registers in the kernel);
+// ALB = -1 reads the mode from the job at run time.
+template <int ALB>
 __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const int tx, const int ty) {
     const Topology &topo = J.topo;
     const FrameDims &dims = J.dims;
@@ -456,8 +459,9 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
     V3 un = pixel_normal_un(v3(r0.x, r0.y, r0.z), v3(r0.w, r1.x, r1.y), v3(r1.z, r1.w, __ldg(&SR[2].x)), abc);
     bool flippedN;
     const V3 n = unit_normal(un, __fsqrt_rn(xdot(un, un)), d, flippedN);
+    const int albedo = ALB >= 0 ? ALB : dims.albedo;
     float3 col;
-    switch (dims.albedo) {
+    switch (albedo) {
         case GVR_ALBEDO_TEXTURED: {
             const float4 r2 = __ldg(SR + 2), r3 = __ldg(SR + 3);
             const float2 tc = texel_coord6(r2.y, r2.z, r2.w, r3.x, r3.y, r3.z, abc, dims.Wt, dims.Ht);
@@ -503,9 +507,9 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
             col = make_float3(1.0f, 1.0f, 1.0f);
             break;
     }
-    const bool lit = dims.albedo != GVR_ALBEDO_NORMAL && dims.albedo != GVR_ALBEDO_UV;
-    const bool shaded = (dims.shading == GVR_SHADING_SHADED && lit) || dims.albedo == GVR_ALBEDO_LIGHTING;
-    if (dims.shading == GVR_SHADING_PHONG && lit && dims.albedo != GVR_ALBEDO_LIGHTING) {
+    const bool lit = albedo != GVR_ALBEDO_NORMAL && albedo != GVR_ALBEDO_UV;
+    const bool shaded = (dims.shading == GVR_SHADING_SHADED && lit) || albedo == GVR_ALBEDO_LIGHTING;
+    if (dims.shading == GVR_SHADING_PHONG && lit && albedo != GVR_ALBEDO_LIGHTING) {
         const float ndl = -(n.x * d.x + n.y * d.y + n.z * d.z);
         const float k = phong_factor(ndl), s = phong_specular(ndl);
         col = make_float3(col.x * k + s, col.y * k + s, col.z * k + s);
@@ -530,10 +534,12 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
 }  // namespace
 
 // One block per tile of one call: grid (tilesX, tilesY, views), views
-// bcBase .. bcBase + gridDim.z - 1.
+// bcBase .. bcBase + gridDim.z - 1.  Compiled for the vertex-colour and the
+// textured albedo and for any mode (ALB = -1).
+template <int ALB>
 __global__ void __launch_bounds__(kTilePix, 5) k_raster(const FwdJob J, int bcBase) {
     pdl_enter();
-    raster_tile(J, bcBase + blockIdx.z, blockIdx.x, blockIdx.y);
+    raster_tile<ALB>(J, bcBase + blockIdx.z, blockIdx.x, blockIdx.y);
 }
 
 // Persistent: a grid sized to the resident capacity pulls (job, view, tile)
@@ -575,17 +581,20 @@ __global__ void __launch_bounds__(kTilePix, 4) k_raster_persistent(const FwdJob 
         for (int w = threadIdx.x; w < words; w += blockDim.x)
             reinterpret_cast<int *>(&sJ)[w] = reinterpret_cast<const int *>(jobs + j)[w];
         __syncthreads();
-        raster_tile(sJ, sBC, sTX, sTY);
+        raster_tile<-1>(sJ, sBC, sTX, sTY);
         __syncthreads();  // shared memory and sItem are reused by the next item
     }
 }
 
 cudaError_t launch_raster(const FwdJob &J, cudaStream_t st) {
     const int BC = J.dims.B * J.dims.C;
+    void (*kernel)(const FwdJob, int) = J.dims.albedo == GVR_ALBEDO_TEXTURED        ? k_raster<GVR_ALBEDO_TEXTURED>
+                                        : J.dims.albedo == GVR_ALBEDO_VERTEX_COLOR ? k_raster<GVR_ALBEDO_VERTEX_COLOR>
+                                                                                   : k_raster<-1>;
     for (int bc0 = 0; bc0 < BC; bc0 += 65535) {  // gridDim.z holds at most 65535 views
         const dim3 grid(J.dims.tilesX, J.dims.tilesY, min(65535, BC - bc0));
         cudaError_t e;
-        GVR_LAUNCH(st, "k_raster", e = launch_pdl(k_raster, grid, dim3(kTilePix), 0, st, J, bc0));
+        GVR_LAUNCH(st, "k_raster", e = launch_pdl(kernel, grid, dim3(kTilePix), 0, st, J, bc0));
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
