@@ -225,7 +225,6 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
     __shared__ int sCandF[kMaxCand][kTilePix];
     __shared__ float sCandZ[kMaxCand][kTilePix];
     float zup = kInf;
-    int nLast = 0;  // kept entries of the last chunk (all of them when nAll <= kChunk)
     int nCand = 0;
     bool spill = false;
     // The view's range of finite, non-negative depth bounds, from the binning
@@ -269,7 +268,6 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
         __syncthreads();  // every warp is done walking the previous chunk; the histogram is clear
         if (keep) atomicAdd(&sHist[q], 1);
         const int nE = __syncthreads_count(keep);
-        nLast = nE;
         if (tid < 32) {  // exclusive prefix of the kBuckets + 1 counts: kPer per lane, one warp scan
             constexpr int kPer = (kBuckets + 1 + 31) / 32;
             int h[kPer];
@@ -405,23 +403,11 @@ __device__ __forceinline__ void raster_tile(const FwdJob &J, const int bc, const
                 abc = t;
             }
         }
-    } else if (nAll <= kChunk) {
-        // more candidates than registers, the tile's entries all still staged
-        // in front-to-back order: test those that may win against the final
-        // bound, up to the first whose bucket lies behind it
-        for (int e = 0; e < nLast; ++e) {
-            if (sBucketLo[e] > zup) break;
-            const Entry E = sE[e];
-            if (u < E.bx0 || u > E.bx1 || v < E.by0 || v > E.by1) continue;
-            if (!may_win(E, px, py, zup)) continue;
-            V3 t;
-            const unsigned long long k = exact_key(x, E.f, t, true);
-            if (k < best) {
-                best = k;
-                abc = t;
-            }
-        }
-    } else {  // more candidates than registers: test every face that may win against the final bound
+    } else {
+        // more candidates than slots (rare): test every entry of the tile
+        // that may win against the final bound, rebuilt from the bins.  (A
+        // second form over the staged entries, for tiles of one chunk, made
+        // the common path spill.)
         for (int e = 0; e < nAll; ++e) {
             const int f = e < nTile ? ws.bins[s0 + e] : bigList[e - nTile];
             const Entry E = make_entry(VF[f], f, tileX0, tileY0, tileW, tileH);
