@@ -22,14 +22,16 @@
 //                comes from one 80-byte record per face that the face pass
 //                of the backward's set-up launch (k_setup) writes.
 //  k_gather_a    per vertex, over its CSR faces: colour grad, position grad
-//                (direct terms) and the vertex-normal gradient gN[v].
+//                (direct terms) and the vertex-normal gradient gN[v]; its
+//                last B*C*27 blocks sum the per-tile SH partials in FP64 in
+//                a fixed order (a separate launch, k_sh_finalize_batched, in
+//                a batched plan).
 //  k_gather_b    per vertex: the normal-adjacency term of :559-615.  The
 //                reference applies, for every pixel, each corner's weight to
 //                every face around that corner (~162 atomics); that sum is
 //                linear in gN, so per face f=(a0,a1,a2) with
 //                s_f = sum of gN over f's distinct vertices, corner r gets
 //                (v[a(r+1)] - v[a(r+2)]) x s_f (= s_f . d cross(v1-v0, v2-v0)/d v_r).
-//  k_sh_finalize sums the per-tile SH partials in FP64 in a fixed order.
 //
 // The shading-term Jacobian dJBCDVerpos (cpp/src/Utils/RendererUtil.h:670-861)
 // is d(barycentrics)/d(vertices) for a fixed ray.  With e1 = v1-v0,
@@ -533,10 +535,49 @@ __device__ __forceinline__ void gather_a_item(const Topology &topo, const float 
     if (useGN) gN[i] = make_float4(acc[3], acc[4], acc[5], 0.0f);
 }
 
-// kGatherLanes threads per vertex (the grid covers B*N*kGatherLanes threads).
-__global__ void k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc, float *__restrict__ vpos_grad,
-                           float *__restrict__ vcol_grad, float4 *__restrict__ gN, int useCol, int useGN) {
+// One block per (batch, view, coefficient), reading that coefficient's row
+// of tile partials: thread i sums tiles i, i+256, ... (FP32 with
+// compensation), then a fixed-order FP64 reduction (warp shuffles, then the
+// eight warp sums in order) finishes, so the result is deterministic and
+// FP64-accurate at FP32 cost.
+__device__ __forceinline__ void sh_finalize_block(const float *__restrict__ partial, float *__restrict__ sh_grad,
+                                                  int tilesPerView, int shaded, int blk) {
+    __shared__ double red[8];
+    const int bc = blk / 27, k = blk % 27;
+    float s = 0.0f, comp = 0.0f;
+    if (shaded)
+        for (int t = threadIdx.x; t < tilesPerView; t += 256) {
+            float hi, lo;
+            two_sum(s, partial[((size_t)bc * 27 + k) * tilesPerView + t], hi, lo);
+            s = hi;
+            comp += lo;
+        }
+    double d = (double)s + (double)comp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += red[w];
+        sh_grad[(size_t)bc * 27 + k] = (float)t;
+    }
+}
+
+// kGatherLanes threads per vertex (the first gatherBlocks blocks cover
+// B*N*kGatherLanes threads); the blocks after them are the SH sums, one per
+// (batch, view, coefficient), which need only the pixel kernel's partials
+// too: run in this grid they leave the chain one launch shorter.
+__global__ void __launch_bounds__(256) k_gather_a(const Topology topo, int B, const float *__restrict__ faceAcc,
+                                                  float *__restrict__ vpos_grad, float *__restrict__ vcol_grad,
+                                                  float4 *__restrict__ gN, int useCol, int useGN, int gatherBlocks,
+                                                  const float *__restrict__ shPartial, float *__restrict__ sh_grad,
+                                                  int tilesPerView, int shaded) {
     pdl_enter();
+    if ((int)blockIdx.x >= gatherBlocks) {
+        sh_finalize_block(shPartial, sh_grad, tilesPerView, shaded, blockIdx.x - gatherBlocks);
+        return;
+    }
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t / kGatherLanes), sub = (int)(t % kGatherLanes);
     gather_a_item<kGatherLanes>(topo, faceAcc, vpos_grad, vcol_grad, gN, useCol, useGN, i, sub, i < B * topo.N);
@@ -596,41 +637,6 @@ __global__ void __launch_bounds__(256) k_gather_batched(const BwdJob *__restrict
                          J.useCol, J.shaded, i, 0, true);
     else if (J.shaded)
         gather_b_item<1>(J.topo, J.io.verts, J.ws.gN, J.vpos_grad, i, 0, true);
-}
-
-// One block per (batch, view, coefficient), reading that coefficient's row
-// of tile partials: thread i sums tiles i, i+256, ... (FP32 with
-// compensation), then a fixed-order FP64 reduction (warp shuffles, then the
-// eight warp sums in order) finishes, so the result is deterministic and
-// FP64-accurate at FP32 cost.
-__device__ __forceinline__ void sh_finalize_block(const float *__restrict__ partial, float *__restrict__ sh_grad,
-                                                  int tilesPerView, int shaded, int blk) {
-    __shared__ double red[8];
-    const int bc = blk / 27, k = blk % 27;
-    float s = 0.0f, comp = 0.0f;
-    if (shaded)
-        for (int t = threadIdx.x; t < tilesPerView; t += 256) {
-            float hi, lo;
-            two_sum(s, partial[((size_t)bc * 27 + k) * tilesPerView + t], hi, lo);
-            s = hi;
-            comp += lo;
-        }
-    double d = (double)s + (double)comp;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < 8; ++w) t += red[w];
-        sh_grad[(size_t)bc * 27 + k] = (float)t;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_sh_finalize(const float *__restrict__ partial, float *__restrict__ sh_grad,
-                                                     int tilesPerView, int shaded) {
-    pdl_enter();
-    sh_finalize_block(partial, sh_grad, tilesPerView, shaded, blockIdx.x);
 }
 
 // One block per (job, batch, view, coefficient) of a batched plan.
@@ -776,22 +782,19 @@ cudaError_t launch_backward(const Topology &topo, const FrameDims &dims, const B
     const bool albpos = (a.flags & GVR_BACKWARD_ALBEDO_POSITION) != 0;
     CallPixels call{topo, dims, ws, io, st};
     if ((err = visit_variant(dims.albedo, shaded, target, albpos, call))) return err;
-    const int useCol = dims.albedo == GVR_ALBEDO_VERTEX_COLOR, useGN = shaded;
+    const int useCol = dims.albedo == GVR_ALBEDO_VERTEX_COLOR, useGN = shaded, shadedFlag = shaded;
+    const int gatherBlocks = blocks((size_t)B * N * kGatherLanes, 256);
     GVR_LAUNCH(st, "k_gather_a",
-               err = launch_pdl(k_gather_a, dim3(blocks((size_t)B * N * kGatherLanes, 256)), dim3(256), 0, st, topo, B,
+               err = launch_pdl(k_gather_a, dim3(gatherBlocks + B * C * 27), dim3(256), 0, st, topo, B,
                                 reinterpret_cast<const float *>(ws.faceAcc), a.vertex_pos_grad, a.vertex_color_grad,
-                                ws.gN, useCol, useGN));
+                                ws.gN, useCol, useGN, gatherBlocks, (const float *)ws.shPartial, a.sh_coeff_grad, T,
+                                shadedFlag));
     if (err) return err;
     if (shaded) {
         GVR_LAUNCH(st, "k_gather_b",
                    err = launch_pdl(k_gather_b, dim3(blocks((size_t)B * N * kGatherLanes, 256)), dim3(256), 0, st,
                                     topo, B, a.vertex_pos, (const float4 *)ws.gN, a.vertex_pos_grad));
-        if (err) return err;
     }
-    const int shadedFlag = shaded;
-    GVR_LAUNCH(st, "k_sh_finalize",
-               err = launch_pdl(k_sh_finalize, dim3(B * C * 27), dim3(256), 0, st, (const float *)ws.shPartial,
-                                a.sh_coeff_grad, T, shadedFlag));
     return err;
 }
 
