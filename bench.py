@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     ap.add_argument("--views", type=int, default=8, help="views of the workload (profiling runs use fewer)")
-    ap.add_argument("--workload", choices=["multiview", "batched", "fit", "learned", "gemm"], default="multiview",
+    ap.add_argument("--workload", choices=["multiview", "batched", "fit", "learned", "gemm", "atomics"],
+                    default="multiview",
                     help="multiview: the fwd+bwd step above (default); batched: 64 uneven meshes through one "
                          "plan (forward + backward), against the same jobs as one call each; fit: plain "
                          "analysis-by-synthesis fits of the morphable model; learned: train the proposal "
@@ -753,6 +754,56 @@ def run_gemm_bench(args):
         print(json.dumps(line), flush=True)
 
 
+def run_atomics_bench(args):
+    """The L2's rate of fire-and-forget FP32 reductions on this GPU: the peak
+    that the scatter kernels' reduction requests are read against.  Every
+    addition of gvr_probe_reductions goes to its own pseudo-random 32-byte
+    sector of a 64 MiB buffer (it stays in L2), so one addition is one L2
+    reduction request; scalar and 16-byte (float4) additions, at 1 to 16
+    resident blocks of 256 threads per SM.  CUDA events, median of
+    `--steps` launches after warm-up."""
+    import torch
+    from gvr import _lib
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    words = 16 << 20
+    buf = torch.zeros(words, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    rounds = 64
+    rows = []
+    for vec in (0, 1):
+        for per_sm in (1, 2, 4, 8, 16):
+            grid = sms * per_sm
+
+            def launch():
+                _lib.check(L.gvr_probe_reductions(ctypes.c_void_p(buf.data_ptr()), words, vec, rounds, grid, sp))
+
+            for _ in range(max(3, args.warmup)):
+                launch()
+            ts = []
+            for _ in range(max(5, args.steps)):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                launch()
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = statistics.median(ts)
+            n = grid * 256 * rounds
+            rows.append({"bytes_per_addition": 16 if vec else 4, "blocks_per_sm": per_sm, "additions": n, "ms": ms,
+                         "g_reductions_per_s": n / ms / 1e6, "gb_per_s": n * (16 if vec else 4) / ms / 1e6})
+    best = {b: max(r["g_reductions_per_s"] for r in rows if r["bytes_per_addition"] == b) for b in (4, 16)}
+    line = {"metric": "L2 FP32 reduction rate, random 32-byte sectors (peak for the scatter kernels)",
+            "value": best[16], "unit": "G reductions/s (16-byte)", "n_gpus": 1, "steps": max(5, args.steps),
+            "warmup": max(3, args.warmup), "higher_is_better": True, "scaling": "none", "vs_baseline": None,
+            "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": "gvr_probe_reductions over a 64 MiB buffer, 64 additions per thread", "sms": sms},
+            "g_reductions_per_s_4byte": best[4], "g_reductions_per_s_16byte": best[16], "rows": rows}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -763,6 +814,8 @@ def main():
         run_fit_bench(args)
     elif args.workload == "gemm":
         run_gemm_bench(args)
+    elif args.workload == "atomics":
+        run_atomics_bench(args)
     else:
         run_gvr(args)
     if int(os.environ.get("WORLD_SIZE", "1")) > 1:

@@ -7,6 +7,9 @@
 #include <string>
 #include <vector>
 
+#include <cstdint>
+
+#include "gvr.h"
 #include "gvr_profile.h"
 
 namespace gvr {
@@ -55,6 +58,20 @@ void drain_locked() {
 }
 
 }  // namespace
+
+// Every thread walks a linear congruential sequence of sector indices; the
+// sector's first float (or float4) takes the addition.  Indices stay below
+// `sectors`, so every access lies in the buffer.
+__global__ void __launch_bounds__(256) k_probe_reductions(float *__restrict__ buf, unsigned sectors, int vector4,
+                                                          int rounds) {
+    unsigned h = (blockIdx.x * 256u + threadIdx.x) * 2654435761u + 12345u;
+    for (int r = 0; r < rounds; ++r) {
+        h = h * 1664525u + 1013904223u;
+        const size_t s = (size_t)(h % sectors) * 8;
+        if (vector4) atomicAdd(reinterpret_cast<float4 *>(buf + s), make_float4(1.0f, 1.0f, 1.0f, 1.0f));
+        else atomicAdd(buf + s, 1.0f);
+    }
+}
 
 KernelScope::KernelScope(cudaStream_t st, const char *name) : st_(st), name_(name) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -105,5 +122,15 @@ int gvr_profile_read(GvrKernelTime *out, int capacity) {
 }
 
 long long gvr_launch_count(void) { return gvr::g_launches.load(); }
+
+int gvr_probe_reductions(float *buf, long long words, int vector4, int rounds, int grid, void *stream) {
+    if (!buf || words < 8 || words % 8 != 0 || words / 8 > 0xffffffffll || rounds < 1 || grid < 1 ||
+        (reinterpret_cast<uintptr_t>(buf) & 31) != 0)
+        return GVR_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    GVR_LAUNCH(st, "k_probe_reductions",
+               gvr::k_probe_reductions<<<grid, 256, 0, st>>>(buf, (unsigned)(words / 8), vector4, rounds));
+    return cudaGetLastError() == cudaSuccess ? GVR_OK : GVR_ERR_CUDA;
+}
 
 }  // extern "C"

@@ -65,7 +65,7 @@ class GvrKernelTime(ctypes.Structure):
 # Every symbol include/gvr.h declares.
 EXPORTS = ("gvr_create", "gvr_destroy", "gvr_forward", "gvr_backward", "gvr_forward_workspace_size",
            "gvr_backward_workspace_size", "gvr_last_error", "gvr_abi_version", "gvr_debug_rays",
-           "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_backward_noalloc",
+           "gvr_profile_enable", "gvr_profile_read", "gvr_launch_count", "gvr_probe_reductions", "gvr_backward_noalloc",
            "gvr_plan_create", "gvr_plan_forward", "gvr_plan_forward_graph", "gvr_plan_tile_config",
            "gvr_plan_bind_backward", "gvr_plan_backward", "gvr_plan_backward_graph", "gvr_plan_destroy", "gvr_image_gradient", "gvr_image_gaussian3x3",
            # include/gvr_nn.h
@@ -110,6 +110,8 @@ def load(build_if_missing: bool = True):
     L.gvr_profile_read.restype = ctypes.c_int
     L.gvr_launch_count.argtypes = []
     L.gvr_launch_count.restype = ctypes.c_longlong
+    L.gvr_probe_reductions.argtypes = [P, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+    L.gvr_probe_reductions.restype = ctypes.c_int
     L.gvr_backward_noalloc.argtypes = [P, ctypes.POINTER(GvrBackwardArgs), P]
     L.gvr_backward_noalloc.restype = ctypes.c_int
     L.gvr_plan_create.argtypes = [ctypes.POINTER(GvrJob), I32, I32, ctypes.POINTER(P)]

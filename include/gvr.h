@@ -305,6 +305,14 @@ int gvr_profile_read(GvrKernelTime *out, int capacity);
 /* Kernels launched by this library since it was loaded (profiling on or off). */
 long long gvr_launch_count(void);
 
+/* Measurement of the L2's reduction rate, no reference counterpart: `grid`
+ * blocks of 256 threads each issue `rounds` fire-and-forget FP32 additions
+ * (vector4 = 0: one float; 1: one 16-byte float4, as the backward's per-face
+ * accumulators take them) to pseudo-random 32-byte sectors of `buf`
+ * (`words` floats, a multiple of 8), one sector per addition, so that every
+ * addition is one L2 reduction request.  Returns GVR_OK or an error code. */
+int gvr_probe_reductions(float *buf, long long words, int vector4, int rounds, int grid, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,6 +84,17 @@ def test_calls_reject_null(lib):
     assert "bad" in lib.gvr_last_error().decode()
 
 
+def test_reduction_probe_checks_arguments_before_any_launch(lib):
+    # the checks read only the pointer's value: a fake, 32-byte aligned address
+    fake = ctypes.c_void_p(1 << 20)
+    assert lib.gvr_probe_reductions(None, 64, 0, 1, 1, None) == -1
+    assert lib.gvr_probe_reductions(fake, 60, 0, 1, 1, None) == -1           # not whole sectors
+    assert lib.gvr_probe_reductions(fake, 0, 0, 1, 1, None) == -1            # empty
+    assert lib.gvr_probe_reductions(fake, 64, 0, 0, 1, None) == -1           # no rounds
+    assert lib.gvr_probe_reductions(fake, 64, 0, 1, 0, None) == -1           # no blocks
+    assert lib.gvr_probe_reductions(ctypes.c_void_p((1 << 20) + 4), 64, 0, 1, 1, None) == -1  # unaligned
+
+
 def test_error_status_raises(lib):
     from gvr import _lib
     with pytest.raises(_lib.GvrError) as ei:
