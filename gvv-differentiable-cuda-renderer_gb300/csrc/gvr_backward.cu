@@ -494,7 +494,7 @@ __device__ __forceinline__ void lane_group_sum(float (&x)[NV]) {
         for (int k = 0; k < NV; ++k) x[k] += __shfl_xor_sync(0xffffffffu, x[k], o);
 }
 
-constexpr int kGatherLanes = 4;
+constexpr int kGatherLanes = 8;
 
 // Face-accumulator layout (floats): [0..8] position grad of corners 0..2,
 // [9..17] vertex-normal grad of corners 0..2, [20..28] colour grad of corners 0..2.
