@@ -713,7 +713,7 @@ cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
     if (err != cudaSuccess) return err;
     if ((err = launch_vertices(J, st)) != cudaSuccess) return err;
     const size_t nvf = (size_t)B * C * J.topo.F;
-    GVR_LAUNCH(st, "k_bin_count", err = launch_pdl(k_bin_count, dim3(blocks(nvf, 256)), dim3(256), 0, st, J));
+    GVR_LAUNCH(st, "k_bin_count", err = launch_pdl(k_bin_count, dim3(blocks(nvf, 128)), dim3(128), 0, st, J));
     if (err != cudaSuccess) return err;
     const int nt = B * C * T;
     constexpr int kScanBlocks = 16;  // beyond this many blocks the re-added prefixes outweigh the parallelism
@@ -726,7 +726,7 @@ cudaError_t launch_forward(const FwdJob &J, cudaStream_t st) {
                    err = launch_pdl(k_scan_tiles_one, dim3(1), dim3(1024), 0, st, (const int *)J.ws.tileCount,
                                     J.ws.tileStart, nt));
     if (err != cudaSuccess) return err;
-    GVR_LAUNCH(st, "k_bin_fill", err = launch_pdl(k_bin_fill, dim3(blocks(nvf, 256)), dim3(256), 0, st, J));
+    GVR_LAUNCH(st, "k_bin_fill", err = launch_pdl(k_bin_fill, dim3(blocks(nvf, 128)), dim3(128), 0, st, J));
     if (err != cudaSuccess) return err;
     return launch_raster(J, st);
 }
