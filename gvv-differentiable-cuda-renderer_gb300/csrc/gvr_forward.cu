@@ -664,7 +664,7 @@ cudaError_t launch_setup(SetupArgs a, cudaStream_t st) {
     const long long n = (long long)a.B * a.F + a.views + zt;
     if (n == 0) return cudaSuccess;
     cudaError_t err;
-    GVR_LAUNCH(st, "k_setup", err = launch_pdl(k_setup, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, a));
+    GVR_LAUNCH(st, "k_setup", err = launch_pdl(k_setup, dim3((unsigned)((n + 127) / 128)), dim3(128), 0, st, a));
     return err;
 }
 
