@@ -59,7 +59,8 @@ def parse():
                          "plan (forward + backward), against the same jobs as one call each; fit: plain "
                          "analysis-by-synthesis fits of the morphable model; learned: train the proposal "
                          "network, then fit from its proposals against the plain fit; gemm: the proposal "
-                         "network's GEMM shapes on the tcgen05 kernel and on torch.matmul")
+                         "network's GEMM shapes on the tcgen05 kernel and on torch.matmul; atomics: the L2's "
+                         "FP32 reduction rate, the peak the scatter kernels' atomics are read against")
     ap.add_argument("--meshes", type=int, default=64, help="meshes of the batched workload")
     ap.add_argument("--fits", type=int, default=1000, help="held-out seeds of the fit / learned workloads")
     ap.add_argument("--train-renders", type=int, default=1_000_000, help="renders the proposal network trains on")
